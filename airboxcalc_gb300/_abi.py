@@ -1,0 +1,128 @@
+"""ctypes binding of libairbox.so (include/airbox.h).
+
+The library is built in-tree by ``airboxcalc_gb300.build``.  Loading fails
+loudly when it is missing: there is no CPU fallback for any compute call.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libairbox.so")
+
+# status codes (abx_status)
+OK = 0
+ERR_NO_TRIANGLES, ERR_SAME_AXIS, ERR_GRID_TOO_LARGE, ERR_NO_OPENING, ERR_OPENING_TOO_SMALL = 1, 2, 3, 4, 5
+ERR_SEAL_OUTSIDE, ERR_LEAK, ERR_LID_TOO_LOW, ERR_BAD_OUTLET, ERR_UNSTABLE = 6, 7, 8, 9, 10
+ERR_NOT_PREPARED, ERR_CANCELLED = 11, 12
+ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_OUT_OF_MEMORY = 20, 21, 22
+
+STORAGE = {"f32": 0, "f32exact": 1, "f16": 2, "bf16": 3, "f64": 4}
+
+# Every symbol include/airbox.h declares.
+EXPORTS = [
+    "abx_last_error", "abx_abi_version", "abx_device_count", "abx_parse_stl", "abx_prepare", "abx_geom_free",
+    "abx_geom_get_info", "abx_geom_get_masks", "abx_geom_get_fine", "abx_sim_create", "abx_sim_free",
+    "abx_sim_get_info", "abx_sim_reset", "abx_sim_step", "abx_sim_run", "abx_sim_get_f", "abx_sim_set_f",
+    "abx_sim_get_acc", "abx_sim_evaluate", "abx_simulate", "abx_sim_set_timing", "abx_sim_get_timing",
+]
+
+
+class PrepareParams(C.Structure):
+    _fields_ = [("dx", C.c_double), ("seal_axis", C.c_int), ("seal_sign", C.c_double), ("seal", C.c_double),
+                ("inlet_axis", C.c_int), ("inlet_sign", C.c_double), ("inlet_yaw", C.c_double),
+                ("pleat", C.c_double), ("has_click", C.c_int), ("click", C.c_double * 3),
+                ("has_outlet", C.c_int), ("outlet_center", C.c_double * 3), ("outlet_diameter", C.c_double),
+                ("outlet_height", C.c_double), ("max_cells", C.c_double), ("device", C.c_int)]
+
+
+class GeomInfo(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("N", C.c_int64), ("nf", C.c_int),
+                ("top", C.c_int), ("jm", C.c_int), ("kw0", C.c_int), ("kf", C.c_int),
+                ("n_holes", C.c_int), ("n_open", C.c_int), ("af", C.c_int), ("n_out", C.c_int),
+                ("leak_cells", C.c_int), ("pleat_ok", C.c_int),
+                ("h", C.c_double), ("origin", C.c_double * 3), ("mn", C.c_double * 3), ("mx", C.c_double * 3),
+                ("pleat", C.c_double), ("volume_l", C.c_double), ("inlet_cm2", C.c_double),
+                ("filter_cm2", C.c_double), ("outlet_cm2", C.c_double), ("outlet_cm2_real", C.c_double),
+                ("frame_cy", C.c_double), ("frame_sy", C.c_double), ("kernel_launches", C.c_int64),
+                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64)]
+
+
+class RunParams(C.Structure):
+    _fields_ = [("K", C.c_double), ("aniso", C.c_double), ("u", C.c_double), ("tau", C.c_double),
+                ("steps", C.c_int), ("avg", C.c_int), ("every", C.c_int), ("storage", C.c_int)]
+
+
+class SimInfo(C.Structure):
+    _fields_ = [("NF", C.c_int), ("Ain", C.c_int), ("Af", C.c_int), ("Lp", C.c_int), ("n_layer_m", C.c_int),
+                ("n_layer_t", C.c_int), ("u0", C.c_double), ("tau0", C.c_double), ("sig", C.c_double),
+                ("aniso", C.c_double), ("cs2s", C.c_double), ("uface", C.c_double), ("step", C.c_int),
+                ("nacc", C.c_int), ("Np", C.c_int64), ("state_bytes", C.c_int64)]
+
+
+class Progress(C.Structure):
+    _fields_ = [("step", C.c_int), ("steps", C.c_int), ("gamma", C.c_double), ("mass_ratio", C.c_double),
+                ("elapsed_s", C.c_double), ("eta_s", C.c_double), ("mlups", C.c_double)]
+
+
+PROGRESS_FN = C.CFUNCTYPE(C.c_int, C.POINTER(Progress), C.c_void_p)
+
+
+class Metrics(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("gamma", "gammaCore", "lowCore", "highCore", "reverse", "maxToMean",
+                                          "zeta", "inlet_cm2", "filter_cm2", "wm", "cm")] + \
+               [(k, C.c_int) for k in ("n", "cn", "pinN", "pbN", "jb")]
+
+
+class Timing(C.Structure):
+    _fields_ = [("step_ms", C.c_double), ("step_launches", C.c_int64), ("step_ms_plain", C.c_double),
+                ("step_launches_plain", C.c_int64), ("run_ms", C.c_double), ("eval_ms", C.c_double),
+                ("cell_updates", C.c_int64), ("kernel_launches", C.c_int64), ("h2d_bytes", C.c_int64),
+                ("d2h_bytes", C.c_int64)]
+
+
+_lib = None
+
+
+def load(build_if_missing: bool = True):
+    """Load libairbox.so (building it first when it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        from . import build as _build
+        _build.build()
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run airboxcalc_gb300.build.build() (needs nvcc)")
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    L.abx_last_error.restype = C.c_char_p
+    L.abx_parse_stl.argtypes = [C.c_char_p, C.c_size_t, vp, C.c_size_t, C.POINTER(C.c_size_t)]
+    L.abx_prepare.argtypes = [vp, C.c_size_t, C.POINTER(PrepareParams), C.POINTER(vp)]
+    L.abx_geom_free.argtypes = [vp]
+    L.abx_geom_free.restype = None
+    L.abx_geom_get_info.argtypes = [vp, C.POINTER(GeomInfo)]
+    L.abx_geom_get_masks.argtypes = [vp] + [vp] * 7
+    L.abx_geom_get_fine.argtypes = [vp, vp, C.c_size_t]
+    L.abx_sim_create.argtypes = [vp, C.POINTER(RunParams), vp, C.POINTER(vp)]
+    L.abx_sim_free.argtypes = [vp]
+    L.abx_sim_free.restype = None
+    L.abx_sim_get_info.argtypes = [vp, C.POINTER(SimInfo)]
+    L.abx_sim_reset.argtypes = [vp]
+    L.abx_sim_step.argtypes = [vp, C.c_int, C.c_int]
+    L.abx_sim_run.argtypes = [vp, PROGRESS_FN, vp]
+    L.abx_sim_get_f.argtypes = [vp, vp]
+    L.abx_sim_set_f.argtypes = [vp, vp]
+    L.abx_sim_get_acc.argtypes = [vp, vp]
+    L.abx_sim_evaluate.argtypes = [vp, C.POINTER(Metrics), vp, vp, C.c_int, C.POINTER(C.c_int)]
+    L.abx_simulate.argtypes = [vp, C.POINTER(RunParams), vp, PROGRESS_FN, vp, C.POINTER(Metrics), vp, vp,
+                               C.c_int, C.POINTER(C.c_int)]
+    L.abx_sim_set_timing.argtypes = [vp, C.c_int]
+    L.abx_sim_get_timing.argtypes = [vp, C.POINTER(Timing)]
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return load().abx_last_error().decode("utf-8", "replace")

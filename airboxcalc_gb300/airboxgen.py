@@ -237,7 +237,12 @@ def random_spec(seed: int, dx: float = 1.5) -> AirboxSpec:
     d = min(d, Ly - 3 * t - 6.0)
     yaw = float(rng.uniform(-30, 30))
     R = 0.5 * d + t
-    stub = max(30.0, R * abs(math.tan(math.radians(yaw))) + 12.0)
+    # The reference searches the opening 1.5 mm behind the front-most point of
+    # the yawed frame (src/engine.js:142), so the stub's end must lie in front
+    # of every rotated box corner: local Z of a point is -sin(yaw) x + cos(yaw) z.
+    sy = math.sin(math.radians(yaw))
+    front = sy * (Lx - 0.5 * Lx) if sy > 0 else -sy * 0.5 * Lx
+    stub = max(30.0, R * abs(math.tan(math.radians(yaw))) + 12.0, front + 8.0)
     frac = float(rng.uniform(0.3, 0.6))
     inner = Lx - 2 * t
     w = frac * inner

@@ -1,0 +1,92 @@
+// lbm_iface.h - argument blocks and launchers shared by the host code
+// (api.cpp) and the kernel translation units.  Plain C++, no CUDA headers
+// beyond the runtime's stream type.
+#pragma once
+#include <cuda_runtime_api.h>
+#include <stdint.h>
+
+namespace abx {
+
+struct StepArgs {
+  void *f;                 // populations A[19][Np], storage type of the run
+  const uint32_t *mask;    // Np cell mask words
+  const uint32_t *seg;     // fluid segment bases (32 cells along k each)
+  uint32_t nseg;
+  int64_t Np;
+  void *acc;               // averages [4][Np] (float, or double for the float64 run)
+  const float *ns;         // partial bounce-back per padded cell, or null
+  const int *status;       // nonzero once the run went unstable: steps become no-ops
+  long long off[19];       // pull offset of direction q in the padded layout
+  double u0, tau0, sig, aniso, cs2s;
+};
+
+struct StateArgs {
+  void *f;
+  const uint32_t *mask;
+  int64_t Np;
+  void *acc;
+  const int64_t *cells;    // padded index of fluid cell a (the reference's compact order)
+  int64_t ncells;
+  int *status;
+  int form;                // 0: "out" form (even steps done), 1: "in" form
+  long long off[19];
+};
+
+struct ProbeArgs {
+  const int64_t *plist;    // padded indices: layer jm cells, then layer top+1 cells
+  int nM, nT;
+  int step, slot;
+  double Ain, u0;
+  double *hist;            // 4 doubles per slot: step, gamma, massRatio, outflow
+};
+
+struct EvalArgs {
+  int nx, ny, nz;
+  int64_t nzp;
+  int jm, jb, nacc;
+  double u0;
+  const uint8_t *opening;  // nx*ny
+  const float *ns;         // padded, or null
+  float *fmap;             // nx*nz, or null
+  double *out;             // 13 doubles
+};
+
+// Launchers (defined in lbm_fast.cu / lbm_exact.cu).  storage: abx_storage value.
+cudaError_t launch_step(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, cudaStream_t st);
+cudaError_t launch_init(int storage, const StateArgs &a, cudaStream_t st);
+cudaError_t launch_get_f(int storage, const StateArgs &a, float *out, cudaStream_t st);
+cudaError_t launch_set_f(int storage, const StateArgs &a, const float *in, cudaStream_t st);
+cudaError_t launch_get_acc(int storage, const StateArgs &a, float *out, int nacc, cudaStream_t st);
+cudaError_t launch_probe(int storage, const StateArgs &a, const ProbeArgs &p, cudaStream_t st);
+cudaError_t launch_evaluate(int storage, const StateArgs &a, const EvalArgs &e, cudaStream_t st);
+// step kernels of the float32-collision storages (lbm_fast.cu)
+cudaError_t launch_step_fast(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, cudaStream_t st);
+
+// Mask construction (mask.cu): class bytes (0 not fluid, 1 bulk, 2 inlet,
+// 3 outlet, 4 filter; index (i*ny+j)*nz+k) -> padded mask words.
+cudaError_t launch_build_mask(const uint8_t *cls, int nx, int ny, int nz, int64_t nzp, uint32_t *mask,
+                              cudaStream_t st);
+// Scatter compact-order values (ns) to the padded layout.
+cudaError_t launch_scatter_f32(const float *src, const int64_t *cells, int64_t n, float *dst, cudaStream_t st);
+
+// Voxelizer (voxelize.cu), bit-exact with src/engine.js:45-93 and the
+// 27->1 downsample of :127-135.
+struct VoxJob {
+  const float *tris;       // device, local-frame triangles, 9 floats each
+  int64_t ntri;
+  double origin[3];
+  double hf;               // fine cell size h/3
+  int nx, ny, nz;          // coarse grid
+  int kf;                  // fine slice index for the opening search
+};
+struct VoxOut {
+  uint8_t *solid;          // device, nx*ny*nz
+  uint8_t *slice;          // device, nxf*nyf: 1 where fine voxel (i,j,kf) is set
+  uint8_t *fine;           // device, nxf*nyf*nzf or null (tests)
+  int64_t launches = 0;    // kernels launched (filled in)
+  int64_t d2h_bytes = 0;   // bytes read back to the host (filled in)
+};
+// Runs the whole voxelizer; scratch is allocated and freed inside.
+cudaError_t run_voxelizer(const VoxJob &job, VoxOut &out, cudaStream_t st);
+
+}  // namespace abx

@@ -1,0 +1,339 @@
+// lbm_kernels.cuh - step, probe, state and evaluate kernels, templated on the
+// population storage.  Included by lbm_fast.cu (float32 / float16 / bfloat16
+// storage, float32 collision) and lbm_exact.cu (compiled with -fmad=false:
+// float32 storage with cpuStep's float64 collision, and a float64 run).
+//
+// Memory layout in HBM (one simulation):
+//   populations  A[q][p], q = 0..18, p = (i*ny + j)*nzp + k, nzp = nz rounded up to 32
+//                one array only: A-A streaming updates it in place
+//   mask         uint32 per padded cell (see d3q19.cuh)
+//   averages     acc[c][p], c = ux, uy, uz, rho (float32; float64 for the float64 run)
+//   segments     uint32 base index of every 32-cell run along k holding a fluid cell
+//
+// A-A streaming.  The reference pulls f_q(x) = f*_q(x - c_q) from a second
+// array (src/engine.js:272-276, bounce-back from the cell's own opposite
+// population when the neighbour is not fluid).  Here one array holds the
+// state in one of two forms:
+//   "out" form (after an even number of steps): A[opp q][x] = f*_q(x)
+//   "in"  form (after an odd  number of steps): A[q][x + c_q] = f*_q(x) when
+//          x + c_q is fluid, else A[opp q][x] = f*_q(x) (already bounced back)
+// An odd step reads out-form neighbours and writes in-form; an even step reads
+// and writes only its own cell.  Every location a thread reads is written by
+// that same thread only, so no step needs a second array.
+#pragma once
+#include <math.h>
+#include <stdint.h>
+
+#include "d3q19.cuh"
+#include "lbm_iface.h"
+
+namespace abx {
+
+template <class L> __device__ __forceinline__ CollideParams<L> make_params(const StepArgs &a) {
+  CollideParams<L> P;
+  P.u0 = (L)a.u0; P.tau0 = (L)a.tau0; P.sig = (L)a.sig; P.aniso = (L)a.aniso; P.cs2s = (L)a.cs2s;
+  return P;
+}
+
+template <int K, bool ODD, bool ACC, bool HAS_NS>
+__global__ void __launch_bounds__(256) aa_step_kernel(const StepArgs a) {
+  using S = Store<K>;
+  using T = typename S::T;
+  using L = typename S::L;
+  using Acc = typename S::Acc;
+  const uint32_t s = blockIdx.x * 8u + (threadIdx.x >> 5);
+  if (s >= a.nseg) return;
+  if (a.status && *(const volatile int *)a.status) return;
+  const int64_t p = (int64_t)a.seg[s] + (threadIdx.x & 31);
+  const uint32_t m = a.mask[p];
+  if (!(m & kFluidBit)) return;
+  T *f = (T *)a.f;
+  const int64_t Np = a.Np;
+  L fi[19];
+#pragma unroll
+  for (int q = 0; q < 19; q++) {
+    int64_t idx;
+    if (ODD) idx = ((m >> q) & 1u) ? (int64_t)opp(q) * Np + p - a.off[q] : (int64_t)q * Np + p;
+    else idx = (int64_t)q * Np + p;
+    fi[q] = S::ld(f + idx, weight<L>(q));
+  }
+  const uint32_t cls = (m >> kClassShift) & 3u;
+  L nsv = (L)0;
+  if (HAS_NS) nsv = (L)a.ns[p];
+  L fo[19], ux, uy, uz, rho;
+  collide<L, HAS_NS>(fi, cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
+#pragma unroll
+  for (int q = 0; q < 19; q++) {
+    int64_t idx;
+    if (ODD) idx = ((m >> opp(q)) & 1u) ? (int64_t)q * Np + p + a.off[q] : (int64_t)opp(q) * Np + p;
+    else idx = (int64_t)opp(q) * Np + p;
+    S::st(f + idx, fo[q], weight<L>(q));
+  }
+  if (ACC) {
+    Acc *acc = (Acc *)a.acc;
+    acc[p] = (Acc)((L)acc[p] + ux);
+    acc[Np + p] = (Acc)((L)acc[Np + p] + uy);
+    acc[2 * Np + p] = (Acc)((L)acc[2 * Np + p] + uz);
+    acc[3 * Np + p] = (Acc)((L)acc[3 * Np + p] + rho);
+  }
+}
+
+// Post-collision populations f*_q(x) of the current state (either form).
+template <int K>
+__device__ __forceinline__ void read_post_all(const StateArgs &a, int64_t x, double (&f)[19]) {
+  using T = typename Store<K>::T;
+  const T *A = (const T *)a.f;
+  const uint32_t m = a.mask[x];
+#pragma unroll
+  for (int q = 0; q < 19; q++) {
+    const int o = opp(q);
+    int64_t idx = (int64_t)o * a.Np + x;
+    if (a.form && ((m >> o) & 1u)) idx = (int64_t)q * a.Np + x + a.off[q];
+    f[q] = (double)Store<K>::ld(A + idx, weight<typename Store<K>::L>(q));
+  }
+}
+
+// Set every fluid cell to w_q (valid in both forms) and clear the averages.
+template <int K>
+__global__ void init_state_kernel(const StateArgs a) {
+  using S = Store<K>;
+  using T = typename S::T;
+  using L = typename S::L;
+  using Acc = typename S::Acc;
+  T *f = (T *)a.f;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.Np; p += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < 19; q++) S::st(f + (int64_t)q * a.Np + p, weight<L>(q), weight<L>(q));
+    if (a.acc) {
+      Acc *acc = (Acc *)a.acc;
+      for (int c = 0; c < 4; c++) acc[(int64_t)c * a.Np + p] = (Acc)0;
+    }
+  }
+}
+
+// f in the reference's compact layout f[q*NF + a] from the device state.
+template <int K>
+__global__ void get_f_kernel(const StateArgs a, float *out) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < a.ncells; n += (int64_t)gridDim.x * blockDim.x) {
+    double f[19];
+    read_post_all<K>(a, a.cells[n], f);
+    for (int q = 0; q < 19; q++) out[(int64_t)q * a.ncells + n] = (float)f[q];
+  }
+}
+
+// Device state in "out" form from f[q*NF + a].
+template <int K>
+__global__ void set_f_kernel(const StateArgs a, const float *in) {
+  using S = Store<K>;
+  using T = typename S::T;
+  using L = typename S::L;
+  T *f = (T *)a.f;
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < a.ncells; n += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = a.cells[n];
+#pragma unroll
+    for (int q = 0; q < 19; q++) S::st(f + (int64_t)opp(q) * a.Np + x, (L)in[(int64_t)q * a.ncells + n], weight<L>(q));
+  }
+}
+
+// Averages acc[c*NF + a] / nacc, rounded to float32 like the reference's
+// Float32Array division (src/engine.js:356).
+template <int K>
+__global__ void get_acc_kernel(const StateArgs a, float *out, int nacc) {
+  using Acc = typename Store<K>::Acc;
+  const Acc *acc = (const Acc *)a.acc;
+  const double dn = nacc > 1 ? (double)nacc : 1.0;
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < a.ncells; n += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = a.cells[n];
+    for (int c = 0; c < 4; c++) out[(int64_t)c * a.ncells + n] = (float)((double)acc[(int64_t)c * a.Np + x] / dn);
+  }
+}
+
+// ---------------------------------------------------------------- block reductions (1024 threads)
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double nan_max(double a, double b) {
+  if (isnan(a) || isnan(b)) return NAN;
+  return a > b ? a : b;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = nan_max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+// Sum of NV doubles over the block, fixed order (deterministic); result in every thread.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double *sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; i++) v[i] = warp_sum(v[i]);
+  __syncthreads();
+  if (lane == 0)
+    for (int i = 0; i < NV; i++) sh[i * 32 + w] = v[i];
+  __syncthreads();
+  if (w == 0) {
+    for (int i = 0; i < NV; i++) {
+      double t = lane < nw ? sh[i * 32 + lane] : 0.0;
+      t = warp_sum(t);
+      if (lane == 0) sh[i * 32] = t;
+    }
+  }
+  __syncthreads();
+  for (int i = 0; i < NV; i++) v[i] = sh[i * 32];
+  __syncthreads();
+}
+__device__ __forceinline__ double block_max(double v, double *sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double t = lane < nw ? sh[lane] : -INFINITY;
+    t = warp_max(t);
+    if (lane == 0) sh[0] = t;
+  }
+  __syncthreads();
+  v = sh[0];
+  __syncthreads();
+  return v;
+}
+
+// probeCPU + progressInfo (src/engine.js:324-339) for one progress check:
+// vy = my/r of the post-collision populations on layer jm and layer top+1,
+// gamma, mass ratio, and the instability flag (first non-finite outflow).
+// One block of 1024 threads; two passes so that no scratch is needed.
+template <int K>
+__global__ void __launch_bounds__(1024) probe_kernel(const StateArgs a, ProbeArgs pr) {
+  __shared__ double sh[3 * 32];
+  const int np = pr.nM + pr.nT;
+  double v[2] = {0.0, 0.0};  // sw, qo
+  for (int n = threadIdx.x; n < np; n += blockDim.x) {
+    double f[19];
+    read_post_all<K>(a, pr.plist[n], f);
+    double r = 0, my = 0;
+#pragma unroll
+    for (int q = 0; q < 19; q++) { r += f[q]; my += (double)cy(q) * f[q]; }
+    const float vy = (float)(my / r);
+    if (n < pr.nM) v[0] += -(double)vy; else v[1] += -(double)vy;
+  }
+  block_sum<2>(v, sh);
+  const double wm = v[0] / pr.nM, qo = v[1];
+  double d[1] = {0.0};
+  for (int n = threadIdx.x; n < pr.nM; n += blockDim.x) {
+    double f[19];
+    read_post_all<K>(a, pr.plist[n], f);
+    double r = 0, my = 0;
+#pragma unroll
+    for (int q = 0; q < 19; q++) { r += f[q]; my += (double)cy(q) * f[q]; }
+    const float vy = (float)(my / r);
+    d[0] += fabs(-(double)vy - wm);
+  }
+  block_sum<1>(d, sh);
+  if (threadIdx.x == 0) {
+    double *h = pr.hist + 4 * (int64_t)pr.slot;
+    h[0] = pr.step;
+    h[1] = 1 - d[0] / (2 * pr.nM * wm);
+    h[2] = qo / (pr.Ain * pr.u0);
+    h[3] = qo;
+    if (!isfinite(qo) && a.status && *a.status == 0) *(int *)a.status = pr.step;
+  }
+}
+
+// evaluate() metrics (src/engine.js:632-660, 681-685) in one block of 1024
+// threads with float64 sums.  Pass 1: filter-map mean, core mean, inlet and
+// sub-pleat density sums; pass 2: deviations, shares, peak ratio, fmap.
+template <int K>
+__global__ void __launch_bounds__(1024) evaluate_kernel(const StateArgs a, EvalArgs e) {
+  using Acc = typename Store<K>::Acc;
+  __shared__ double sh[6 * 32];
+  const Acc *acc = (const Acc *)a.acc;
+  const int nx = e.nx, ny = e.ny, nz = e.nz;
+  const int64_t nzp = e.nzp;
+  const double dn = e.nacc > 1 ? (double)e.nacc : 1.0;
+  auto P = [&](int i, int j, int k) -> int64_t { return ((int64_t)i * ny + j) * nzp + k; };
+  auto fluid = [&](int64_t p) -> bool {
+    if (!(a.mask[p] & kFluidBit)) return false;
+    return !(e.ns && e.ns[p] > 0.5f);
+  };
+  // mean field as the reference holds it: float32(acc / nacc); the float64 run keeps float64
+  auto mean = [&](int c, int64_t p) -> double {
+    const double m = (double)acc[(int64_t)c * a.Np + p] / dn;
+    if constexpr (sizeof(Acc) == 8) return m;
+    else return (double)(float)m;
+  };
+  auto core = [&](int i, int k) -> bool {
+    if (i < 1 || i > nx - 2 || k < 1 || k > nz - 2) return false;
+    return fluid(P(i, e.jm, k)) && fluid(P(i - 1, e.jm, k)) && fluid(P(i + 1, e.jm, k)) && fluid(P(i, e.jm, k - 1)) &&
+           fluid(P(i, e.jm, k + 1));
+  };
+  const int64_t nxz = (int64_t)nx * nz;
+  // pass 1: sw, n, csum, cn, pin, pinN, pb, pbN
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  double cnt[4] = {0, 0, 0, 0};
+  for (int64_t x = threadIdx.x; x < nxz; x += blockDim.x) {
+    const int i = (int)(x / nz), k = (int)(x % nz);
+    const int64_t p = P(i, e.jm, k);
+    if (fluid(p)) {
+      const double w = -mean(1, p);
+      v[0] += w; cnt[0] += 1;
+      if (core(i, k)) { v[1] += w; cnt[1] += 1; }
+    }
+    const int64_t pb = P(i, e.jb, k);
+    if (fluid(pb)) { v[3] += mean(3, pb); cnt[3] += 1; }
+  }
+  for (int64_t x = threadIdx.x; x < (int64_t)nx * ny; x += blockDim.x) {
+    if (!e.opening[x]) continue;
+    const int i = (int)(x / ny), j = (int)(x % ny);
+    const int64_t p = P(i, j, 1);
+    if (fluid(p)) { v[2] += mean(3, p); cnt[2] += 1; }
+  }
+  double r1[8] = {v[0], v[1], v[2], v[3], cnt[0], cnt[1], cnt[2], cnt[3]};
+  {
+    double t[6];
+    for (int i = 0; i < 6; i++) t[i] = r1[i];
+    block_sum<6>(t, sh);
+    for (int i = 0; i < 6; i++) r1[i] = t[i];
+    double u[2] = {r1[6], r1[7]};
+    block_sum<2>(u, sh);
+    r1[6] = u[0]; r1[7] = u[1];
+  }
+  const double sw = r1[0], csum = r1[1], pin = r1[2], pb = r1[3];
+  const double n = r1[4], cn = r1[5], pinN = r1[6], pbN = r1[7];
+  const double wm = sw / n, cm = csum / cn;
+  // pass 2: dev, cdev, rev, low, high, max
+  double d[5] = {0, 0, 0, 0, 0};
+  double mxr = 0.0;
+  for (int64_t x = threadIdx.x; x < nxz; x += blockDim.x) {
+    const int i = (int)(x / nz), k = (int)(x % nz);
+    const int64_t p = P(i, e.jm, k);
+    if (!fluid(p)) { if (e.fmap) e.fmap[x] = NAN; continue; }
+    const double w = -mean(1, p);
+    d[0] += fabs(w - wm);
+    if (w < 0) d[2] += 1;
+    mxr = nan_max(mxr, w / wm);
+    if (core(i, k)) {
+      d[1] += fabs(w - cm);
+      if (w < 0.5 * cm) d[3] += 1;
+      if (w > 1.5 * cm) d[4] += 1;
+    }
+    if (e.fmap) e.fmap[x] = (float)(w / wm);
+  }
+  block_sum<5>(d, sh);
+  mxr = block_max(mxr, sh);
+  if (threadIdx.x == 0) {
+    double *o = e.out;
+    o[0] = 1 - d[0] / (2 * n * wm);            // gamma
+    o[1] = 1 - d[1] / (2 * cn * cm);           // gammaCore
+    o[2] = d[3] / cn;                          // lowCore
+    o[3] = d[4] / cn;                          // highCore
+    o[4] = d[2] / n;                           // reverse
+    o[5] = mxr;                                // maxToMean
+    o[6] = ((pin / pinN - pb / pbN) / 3) / (0.5 * e.u0 * e.u0);  // zeta
+    o[7] = wm; o[8] = cm; o[9] = n; o[10] = cn; o[11] = pinN; o[12] = pbN;
+  }
+}
+
+}  // namespace abx

@@ -1,0 +1,350 @@
+"""Benchmark of the airbox compute core on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload config2|config1|config3] [--storage f32|f16|bf16]
+
+One bench step is one whole solve of the workload's airbox: the full
+simulate() step loop (6000 LBM steps, the last 2000 averaged, a progress
+probe every 150 steps) and evaluate(), on a geometry already prepared on the
+GPU.  MLUPS counts fluid-cell updates per second, the reference's definition
+(src/engine.js:338).
+
+* ``value``  - MLUPS from CUDA-event device time of the K solves (state and
+  geometry resident in HBM).
+* ``e2e``    - MLUPS through the C ABI with host buffers: every step prepares
+  the geometry from host triangles (H2D, GPU voxelizer, host flood fill),
+  runs the solve and reads KPIs, filter map and history back to the host.
+* ``roofline`` - the fused stream+collide kernel (launches without
+  averaging): 2*19*4 bytes per fluid cell per launch (float32 storage) over
+  its CUDA-event launch time, against the measured HBM copy bandwidth.
+* ``cpu_baseline`` - the oracle's restatement of the reference's cpuStep
+  (single thread, float64 locals as in JavaScript) on the same airbox.
+
+``--impl reference`` times the reference's CPU algorithm (no JavaScript
+runtime exists on this machine, so the C restatement stands in for
+src/engine.js's cpuStep) with every host core, on the same workload.
+Under torchrun the solves run as independent replicas, one per GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MLUPS; time to converged γ/ζ (±1%): FP16+warm-start vs plain FP32 LBM"
+RUN = dict(K=3.0, aniso=10.0, u=0.06, tau=0.51, steps=6000, avg=2000, every=150)
+
+
+def workload(name: str):
+    from airboxcalc_gb300 import airboxgen as ag
+    if name == "config1":
+        spec = ag.config1_spec()
+        return spec, dict(RUN), "config1: 240x120x180 mm airbox, 70 mm inlet + 30 mm stub, dx 4 mm, 6000/2000 steps"
+    if name == "config2":
+        spec = ag.random_spec(1000, dx=1.5)
+        return spec, dict(RUN), "config2: seeded airbox (seed 1000), dx 1.5 mm, 6000 steps / 2000 averaged"
+    if name == "config3":
+        spec = ag.grid_spec(512, 256, 384, dx=0.6)
+        run = dict(RUN, tau=0.505, u=0.05, steps=20000, avg=5000, every=500)
+        return spec, run, "config3: 512x256x384-cell airbox, dx 0.6 mm, 20000 steps / 5000 averaged"
+    raise SystemExit(f"unknown workload {name}")
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ helpers
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max-over-ranks for replica runs under torchrun (gloo on the host)."""
+
+    def __init__(self, ws: int):
+        self.ws = ws
+        self.pg = None
+        if ws > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_tag: str):
+    """DRAM bytes per launch of the step kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+# ------------------------------------------------------------------ CPU legs
+def cpu_baseline(spec, run, nthreads: int, target_s: float = 12.0):
+    """The oracle's cpuStep restatement on the workload's airbox: LBM steps from
+    w_i until about target_s seconds have passed."""
+    from oracle import oracle as O
+    from airboxcalc_gb300 import airboxgen as ag
+    og = O.prepare(ag.build_airbox(spec), spec.prepare_params(), max_cells=1e10)
+    S = O.OracleSim(og, run)
+    f = S.f0()
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        f = S.step(f, kind="f32", nthreads=nthreads)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= target_s or n >= 200:
+            break
+    return S.NF * n / el / 1e6, n, el, S.NF
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3"])
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    a = ap.parse_args()
+    ws, rank, local = dist_env()
+    spec, run, desc = workload(a.workload)
+
+    if a.impl == "reference":
+        if rank != 0:
+            return 0
+        from oracle import oracle as O
+        from airboxcalc_gb300 import airboxgen as ag
+        O.build()
+        cores = os.cpu_count() or 1
+        og = O.prepare(ag.build_airbox(spec), spec.prepare_params(), max_cells=1e10)
+        S = O.OracleSim(og, run)
+        f = S.f0()
+        per_step = 10
+        for _ in range(a.warmup):
+            for _ in range(per_step):
+                f = S.step(f, kind="f32", nthreads=cores)
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            for _ in range(per_step):
+                f = S.step(f, kind="f32", nthreads=cores)
+        el = time.perf_counter() - t0
+        v = S.NF * per_step * a.steps / el / 1e6
+        sample = f"{per_step} LBM steps of the workload airbox per bench step (NF={S.NF}), from w_i"
+        line = {"metric": METRIC, "value": round(v, 3), "unit": "MLUPS", "n_gpus": a.gpus, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": round(el / a.steps * 1e3, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64-locals/f32-storage", "data": "synthetic",
+                "config": {"workload": desc, "lbm_steps_per_bench_step": per_step, "NF": S.NF},
+                "impl": "reference",
+                "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": cores, "kind": "port",
+                                 "sample": sample + "; C restatement of src/engine.js cpuStep (no JavaScript "
+                                 "runtime here), OpenMP over cells"},
+                "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    # ---------------------------------------------------------------- our arm
+    from airboxcalc_gb300 import _abi
+    from airboxcalc_gb300 import airboxgen as ag
+    from airboxcalc_gb300 import engine as E
+    dist = Dist(ws)
+    device = local if ws > 1 else 0
+    tris = ag.build_airbox(spec)
+    p = {**spec.prepare_params(), "maxCells": 1e10, "device": device}
+    runp = {**run, "storage": a.storage}
+    g = E.prepare({"tris": tris, **p})
+    S = E.Simulation(g, runp)
+    NF = S.NF
+    S.set_timing(True)
+
+    def solve():
+        S.reset()
+        S.run()
+        return S.evaluate()
+
+    for _ in range(a.warmup):
+        res = solve()
+    sampler = ClockSampler(device)
+    sampler.start()
+    dist.barrier()
+    S.reset()  # counters and event times cleared; the timed solves follow
+    t_dev = 0.0
+    t_wall0 = time.perf_counter()
+    step_ms = plain_ms = 0.0
+    plain_launches = launches = kernels = 0
+    for _ in range(a.steps):
+        S.reset()
+        S.run()
+        res = S.evaluate()
+        t = S.timing()
+        t_dev += t["run_ms"] + t["eval_ms"]
+        step_ms += t["step_ms"]
+        plain_ms += t["step_ms_plain"]
+        plain_launches += t["step_launches_plain"]
+        launches += t["step_launches"]
+        kernels += t["kernel_launches"]
+    wall = time.perf_counter() - t_wall0
+    dist.barrier()
+    clocks = sampler.stop()
+    t_dev_max = dist.max(t_dev)
+    units = dist.sum(NF * run["steps"] * a.steps)
+    value = units / (t_dev_max * 1e-3) / 1e6
+    ms_per_step = t_dev_max / a.steps
+
+    # end to end through the C ABI with host buffers
+    e2e_times, h2d, d2h = [], 0, 0
+    e2e_kernels = 0
+    for i in range(a.warmup + a.steps):
+        t0 = time.perf_counter()
+        g2 = E.prepare({"tris": tris, **p})
+        S2 = E.Simulation(g2, runp)
+        S2.run()
+        r2 = S2.evaluate()
+        el = time.perf_counter() - t0
+        if i >= a.warmup:
+            e2e_times.append(el)
+            gi, t2 = g2.info, S2.timing()
+            h2d = gi.h2d_bytes + t2["h2d_bytes"]
+            d2h = gi.d2h_bytes + t2["d2h_bytes"]
+            e2e_kernels = gi.kernel_launches + t2["kernel_launches"]
+        del S2, g2
+    e2e_t = dist.max(sum(e2e_times)) / len(e2e_times)
+    e2e = dist.sum(NF * run["steps"]) / e2e_t / 1e6
+
+    # roofline of the fused step kernel (launches without averaging)
+    bytes_per_cell = 2 * 19 * (4 if a.storage == "f32" else 2)
+    avg_launch_ms = plain_ms / max(plain_launches, 1)
+    achieved = bytes_per_cell * NF / (avg_launch_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = ncu_traffic(f"lbm_step_{a.storage}_{a.workload}")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "kernel": f"aa_step_kernel<{a.storage}> (fused pull-stream+collide, A-A in place)",
+                "bytes_per_launch": bytes_per_cell * NF, "avg_launch_us": round(avg_launch_ms * 1e3, 3)}
+
+    line = {"metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": ws, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": a.storage, "data": "synthetic",
+            "config": {"workload": desc, "grid": [g.nx, g.ny, g.nz], "NF": NF, "lbm_steps_per_bench_step": run["steps"],
+                       "averaged_steps": run["avg"], "storage": a.storage,
+                       "state_bytes": int(S.info.state_bytes),
+                       "l2": "state larger than the 129 MB L2, no flush needed" if S.info.state_bytes > 129e6
+                       else "state smaller than L2",
+                       "parallelism": f"replicas x{ws}"},
+            "kpis": {k: round(res["metrics"][k], 6) for k in ("gamma", "gammaCore", "lowCore", "maxToMean", "zeta")},
+            "e2e": {"value": round(e2e, 1), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_t * 1e3, 3)},
+            "roofline": roofline,
+            "gpu_launches": int(kernels),
+            "gpu_launches_e2e_per_step": int(e2e_kernels),
+            "wall_s_timed": round(wall, 3),
+            "clocks": clocks}
+    if rank == 0 and not a.no_cpu_baseline:
+        v, n, el, nf = cpu_baseline(spec, run, 1)
+        line["cpu_baseline"] = {"value": round(v, 3), "unit": "MLUPS", "cores": 1, "kind": "port",
+                                "sample": f"{n} LBM steps of the same airbox (NF={nf}) from w_i in {el:.1f} s, "
+                                          "oracle restatement of src/engine.js cpuStep (float64 locals), 1 thread"}
+    if rank == 0:
+        print(json.dumps(line))
+    dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,205 @@
+/* airbox.h - C ABI of libairbox.so, the GB300 (sm_103a) compute core of the
+ * airbox-flow tool.
+ *
+ * Every entry point replaces one function of the reference's engine surface,
+ * src/engine.js (module.exports at src/engine.js:803), and is named after it.
+ * Plain pointers and sizes only; all host buffers are caller-owned, all device
+ * memory is owned by the opaque handles.  Every call returns an abx_status;
+ * on failure abx_last_error() holds the reference's message text for that
+ * condition (German, as thrown by engine.js) or a CUDA error string.
+ *
+ * Threading: a handle may be used from one thread at a time.  Each simulation
+ * handle owns one CUDA stream; calls block until their GPU work is done.
+ * There is no CPU fallback: without a usable sm_103a GPU every compute call
+ * fails with ABX_ERR_CUDA.
+ */
+#ifndef AIRBOX_H
+#define AIRBOX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ABX_ABI_VERSION 1
+
+/* Status codes.  The first group mirrors the errors engine.js throws. */
+typedef enum {
+  ABX_OK = 0,
+  ABX_ERR_NO_TRIANGLES = 1,      /* src/engine.js:26  "STL enthält keine Dreiecke." */
+  ABX_ERR_SAME_AXIS = 2,         /* src/engine.js:33  seal and inlet on the same axis */
+  ABX_ERR_GRID_TOO_LARGE = 3,    /* src/engine.js:124 grid above the cell cap */
+  ABX_ERR_NO_OPENING = 4,        /* src/engine.js:156 no inlet opening found */
+  ABX_ERR_OPENING_TOO_SMALL = 5, /* src/engine.js:171 opening below 8 cells */
+  ABX_ERR_SEAL_OUTSIDE = 6,      /* src/engine.js:180 seal plane outside the model */
+  ABX_ERR_LEAK = 7,              /* src/engine.js:195 air leaks through a thin wall */
+  ABX_ERR_LID_TOO_LOW = 8,       /* src/engine.js:200 outlet lid lower than a cell */
+  ABX_ERR_BAD_OUTLET = 9,        /* src/engine.js:210 outlet not above the filter */
+  ABX_ERR_UNSTABLE = 10,         /* src/engine.js:335 non-finite flux at a progress check */
+  ABX_ERR_NOT_PREPARED = 11,     /* src/engine.js:796 run without a prepared geometry */
+  ABX_ERR_CANCELLED = 12,        /* progress callback asked to stop (the UI's cancel, src/ui.html:508) */
+  ABX_ERR_INVALID_ARGUMENT = 20, /* bad pointer, size or parameter (no reference counterpart) */
+  ABX_ERR_CUDA = 21,             /* CUDA runtime error; no GPU fallback exists */
+  ABX_ERR_OUT_OF_MEMORY = 22
+} abx_status;
+
+/* Population storage of a simulation. */
+typedef enum {
+  ABX_STORE_F32 = 0,        /* float32 populations, float32 collision (the WGSL lbm_step contract, src/engine.js:378-450) */
+  ABX_STORE_F32_EXACT = 1,  /* float32 populations, float64 collision in cpuStep's exact operation order (src/engine.js:266-321) */
+  ABX_STORE_F16 = 2,        /* binary16 shifted deviations f - w_i, float32 collision */
+  ABX_STORE_BF16 = 3,       /* bfloat16 shifted deviations f - w_i, float32 collision */
+  ABX_STORE_F64 = 4         /* float64 populations and collision (an FP64 run on the GPU) */
+} abx_storage;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *abx_last_error(void);
+int abx_abi_version(void);
+/* Number of CUDA devices visible (0 without a GPU); never fails. */
+int abx_device_count(void);
+
+/* parseSTL (src/engine.js:15-28).  Binary if 84 + 50 n == len, else ASCII
+ * "vertex x y z" records.  Call with out == NULL to get *nfloats (9 per
+ * triangle), then again with cap >= *nfloats. */
+int abx_parse_stl(const void *buf, size_t len, float *out, size_t cap, size_t *nfloats);
+
+/* prepare(p) parameters (src/engine.js:111, fields of src/ui.html:477-479). */
+typedef struct {
+  double dx;                     /* cell size h, mm */
+  int seal_axis;                 /* p.sealAxis 0..2 */
+  double seal_sign;              /* p.sealSign +-1 */
+  double seal;                   /* p.seal, model coordinate of the seal plane */
+  int inlet_axis;                /* p.inletAxis 0..2 */
+  double inlet_sign;             /* p.inletSign +-1 */
+  double inlet_yaw;              /* p.inletYaw, degrees */
+  double pleat;                  /* p.pleat, mm */
+  int has_click; double click[3];            /* p.click (model coordinates) or none */
+  int has_outlet; double outlet_center[3];   /* p.outlet.enabled / .center */
+  double outlet_diameter, outlet_height;     /* p.outlet.diameter / .height */
+  double max_cells;              /* cell cap; the reference's is 4.5e6 (src/engine.js:124) */
+  int device;                    /* CUDA device ordinal */
+} abx_prepare_params;
+
+typedef struct abx_geom abx_geom;
+
+/* prepare(p) (src/engine.js:111-234): frame transform, grid sizing, GPU parity
+ * voxelizer at 3x oversampling with the 27->1 downsample, opening detection,
+ * inlet duct, flood fill, leak check, outlet plane/plenum.  `tris` holds
+ * nfloats model-space floats (9 per triangle) in host memory. */
+int abx_prepare(const float *tris, size_t nfloats, const abx_prepare_params *p, abx_geom **out);
+void abx_geom_free(abx_geom *g);
+
+/* The prepare() return object's scalars and its `summary` (src/engine.js:226-233). */
+typedef struct {
+  int nx, ny, nz; int64_t N;
+  int nf;                 /* fluid cells (g.nf) */
+  int top, jm, kw0, kf;
+  int n_holes, n_open, af, n_out, leak_cells, pleat_ok;
+  double h, origin[3], mn[3], mx[3], pleat;
+  double volume_l, inlet_cm2, filter_cm2, outlet_cm2, outlet_cm2_real;
+  double frame_cy, frame_sy;  /* cos/sin of the yaw used by the frame */
+  int64_t kernel_launches;    /* kernels prepare() launched */
+  int64_t h2d_bytes, d2h_bytes;  /* bytes prepare() copied host->device / device->host */
+} abx_geom_info;
+int abx_geom_get_info(const abx_geom *g, abx_geom_info *out);
+/* Host copies of g.solid / g.fluid / g.outlet (N bytes each, index (i*ny+j)*nz+k),
+ * g.opening (nx*ny) and g.xc/g.dc/g.zc (float).  Any pointer may be NULL. */
+int abx_geom_get_masks(const abx_geom *g, uint8_t *solid, uint8_t *fluid, uint8_t *opening, uint8_t *outlet,
+                       float *xc, float *dc, float *zc);
+/* The fine (3x) voxel grid of voxelize() (src/engine.js:45-93), nxf*nyf*nzf bytes,
+ * recomputed on the GPU on demand.  For grids up to 2^31 fine voxels. */
+int abx_geom_get_fine(const abx_geom *g, uint8_t *fine, size_t cap);
+
+/* simulate() parameters (src/engine.js:237, fields of src/ui.html:502-504). */
+typedef struct {
+  double K, aniso, u, tau;       /* filter resistance, cross-pleat factor, inlet speed, relaxation time */
+  int steps, avg, every;         /* time steps, averaged tail, progress interval */
+  int storage;                   /* abx_storage */
+} abx_run_params;
+
+typedef struct abx_sim abx_sim;
+
+/* setupSim(g, p) (src/engine.js:239-264) plus device state: populations set
+ * to w_i, averages cleared.  `ns` is the optional partial bounce-back field
+ * (src/engine.js:238, 313-317): NF floats in fluid-cell order, or NULL. */
+int abx_sim_create(abx_geom *g, const abx_run_params *p, const float *ns, abx_sim **out);
+void abx_sim_free(abx_sim *s);
+
+typedef struct {
+  int NF, Ain, Af, Lp, n_layer_m, n_layer_t;
+  double u0, tau0, sig, aniso, cs2s, uface;
+  int step, nacc;               /* steps done, steps accumulated */
+  int64_t Np;                   /* padded cells held on the device */
+  int64_t state_bytes;          /* device bytes of populations + averages */
+} abx_sim_info;
+int abx_sim_get_info(const abx_sim *s, abx_sim_info *out);
+
+/* Back to the initial state (f = w_i, averages and history cleared). */
+int abx_sim_reset(abx_sim *s);
+
+/* n calls of cpuStep (src/engine.js:266-321) / lbm_step (:378-450), adding to
+ * the averages when `accumulate` is nonzero. */
+int abx_sim_step(abx_sim *s, int n, int accumulate);
+
+/* Progress report of simulate()'s onProgress (src/engine.js:330-339,351-354). */
+typedef struct {
+  int step, steps;
+  double gamma, mass_ratio, elapsed_s, eta_s, mlups;
+} abx_progress;
+/* Return nonzero to cancel the run (ABX_ERR_CANCELLED). */
+typedef int (*abx_progress_fn)(const abx_progress *info, void *user);
+
+/* The simulate() step loop (src/engine.js:341-358, simulateGPU :613-630):
+ * steps with the averaging window, a probe every `every` steps, and the
+ * instability check of progressInfo (:335).  With cb == NULL the host does
+ * not wait for the GPU until the end. */
+int abx_sim_run(abx_sim *s, abx_progress_fn cb, void *user);
+
+/* Post-collision populations f (19*NF floats, f[i*NF + a]) in the reference's
+ * layout, and the way back (for self-tests and warm starts). */
+int abx_sim_get_f(abx_sim *s, float *f);
+int abx_sim_set_f(abx_sim *s, const float *f);
+/* Time-averaged fields acc[comp*NF + a], comp = ux, uy, uz, rho, divided by
+ * the accumulated step count as simulate() does (src/engine.js:356). */
+int abx_sim_get_acc(abx_sim *s, float *acc);
+
+/* evaluate() metrics (src/engine.js:681-685). */
+typedef struct {
+  double gamma, gammaCore, lowCore, highCore, reverse, maxToMean, zeta, inlet_cm2, filter_cm2;
+  double wm, cm; int n, cn, pinN, pbN, jb;
+} abx_metrics;
+/* evaluate() (src/engine.js:632-691) on the device: filter map at layer jm,
+ * gamma, gamma core, lowCore, highCore, reverse, maxToMean and zeta, with
+ * float64 sums.  fmap (nx*nz floats, w/mean or NaN) and hist (3 doubles
+ * [step, gamma, massRatio] per progress check, hist_cap rows) may be NULL. */
+int abx_sim_evaluate(abx_sim *s, abx_metrics *m, float *fmap, double *hist, int hist_cap, int *nhist);
+
+/* simulate(g, p, onProgress, ns) in one call (src/engine.js:341-358):
+ * setupSim, the step loop and evaluate. */
+int abx_simulate(abx_geom *g, const abx_run_params *p, const float *ns, abx_progress_fn cb, void *user,
+                 abx_metrics *m, float *fmap, double *hist, int hist_cap, int *nhist);
+
+/* Accounting of a simulation handle since its last reset (no reference
+ * counterpart; used for roofline and end-to-end figures).  Device times are
+ * measured with CUDA events on the handle's stream while timing is enabled;
+ * counters are kept always. */
+typedef struct {
+  double step_ms;                 /* device time of all step-kernel launches */
+  int64_t step_launches;
+  double step_ms_plain;           /* ... of the launches that do not accumulate averages */
+  int64_t step_launches_plain;
+  double run_ms;                  /* device time of abx_sim_run calls */
+  double eval_ms;                 /* device time of abx_sim_evaluate calls */
+  int64_t cell_updates;           /* fluid-cell updates done (NF per step) */
+  int64_t kernel_launches;        /* kernels launched by this handle */
+  int64_t h2d_bytes, d2h_bytes;   /* bytes copied host->device / device->host by this handle */
+} abx_sim_timing;
+int abx_sim_set_timing(abx_sim *s, int enabled);
+int abx_sim_get_timing(const abx_sim *s, abx_sim_timing *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AIRBOX_H */

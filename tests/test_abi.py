@@ -1,0 +1,66 @@
+"""libairbox.so loads, exports every entry point include/airbox.h declares,
+and its host-only STL parser agrees with the oracle (no GPU needed)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from airboxcalc_gb300 import _abi as A
+from airboxcalc_gb300 import airboxgen as ag
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = np.load(os.path.join(ROOT, "tests", "golden", "airbox_cfd_golden.npz"))
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "airbox.h")).read()
+    return sorted(set(re.findall(r"\b(abx_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_header_and_binding_agree():
+    assert header_symbols() == sorted(A.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol():
+    L = A.load()
+    for name in header_symbols():
+        assert hasattr(L, name), name
+    assert L.abx_abi_version() == 1
+
+
+@pytest.mark.parametrize("key", ["stl_binary", "stl_ascii"])
+def test_parse_stl_matches_oracle_and_reference(key):
+    from airboxcalc_gb300 import engine as E
+    buf = GOLD[key].tobytes()
+    got = E.parseSTL(buf)
+    assert np.array_equal(got, O.parse_stl(buf))
+    assert np.array_equal(got, GOLD[key + "_parsed"])
+
+
+def test_parse_stl_errors():
+    from airboxcalc_gb300 import engine as E
+    with pytest.raises(E.AirboxError) as ei:
+        E.parseSTL(b"solid nothing\nendsolid\n")
+    assert ei.value.code == A.ERR_NO_TRIANGLES and "keine Dreiecke" in str(ei.value)
+    weird = b"vertex 1.2.3 0 0 vertex 1 0 0 vertex 0 1 0 vertex 9 9\nvertex 1 2 3"
+    a, b = E.parseSTL(weird), O.parse_stl(weird)
+    assert np.array_equal(np.isnan(a), np.isnan(b)) and np.array_equal(a[~np.isnan(a)], b[~np.isnan(b)])
+
+
+def test_binary_stl_of_generated_airbox_roundtrips():
+    from airboxcalc_gb300 import engine as E
+    tris = ag.build_airbox(ag.random_spec(3, dx=3.0))
+    assert np.array_equal(E.parseSTL(ag.to_binary_stl(tris)), tris.ravel())
+
+
+def test_compute_calls_fail_loudly_without_gpu():
+    from airboxcalc_gb300 import engine as E
+    if A.load().abx_device_count() > 0:
+        pytest.skip("a GPU is visible")
+    spec = ag.config1_spec()
+    with pytest.raises(E.AirboxError) as ei:
+        E.prepare({"tris": ag.build_airbox(spec), **spec.prepare_params()})
+    assert ei.value.code == A.ERR_CUDA
