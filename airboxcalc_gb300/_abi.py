@@ -86,16 +86,19 @@ _lib = None
 
 
 def load(build_if_missing: bool = True):
-    """Load libairbox.so (building it first when it is missing or stale)."""
+    """Load libairbox.so (building it first when it is missing or stale).
+
+    ABX_LIBRARY, when set, names another build of the library to load."""
     global _lib
     if _lib is not None:
         return _lib
-    if build_if_missing:
+    path = os.environ.get("ABX_LIBRARY", LIB_PATH)
+    if build_if_missing and path == LIB_PATH:
         from . import build as _build
         _build.build()
-    if not os.path.exists(LIB_PATH):
-        raise RuntimeError(f"{LIB_PATH} is missing: run airboxcalc_gb300.build.build() (needs nvcc)")
-    L = C.CDLL(LIB_PATH)
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run airboxcalc_gb300.build.build() (needs nvcc)")
+    L = C.CDLL(path)
     vp = C.c_void_p
     L.abx_last_error.restype = C.c_char_p
     L.abx_parse_stl.argtypes = [C.c_char_p, C.c_size_t, vp, C.c_size_t, C.POINTER(C.c_size_t)]

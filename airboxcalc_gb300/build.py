@@ -58,22 +58,27 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(s) <= t for s in _sources())
 
 
-def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
-    if not force and up_to_date():
+def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False, extra_nvcc=(), out: str = None,
+          build_dir: str = None) -> str:
+    """Compile and link; ``extra_nvcc``/``out``/``build_dir`` build a variant elsewhere
+    (e.g. with different -D tuning macros) without touching the in-tree library."""
+    lib = out or LIB
+    bdir = build_dir or BUILD
+    if not force and out is None and up_to_date():
         return LIB
     nvcc = _nvcc()
     cuda_inc = os.path.join(_cuda_home(nvcc), "include")
-    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(bdir, exist_ok=True)
 
     def compile_unit(unit):
         src, extra = unit
-        obj = os.path.join(BUILD, src + ".o")
+        obj = os.path.join(bdir, src + ".o")
         path = os.path.join(CSRC, src)
         if extra is None:
             cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall",
                    "-I" + cuda_inc, "-I" + INCLUDE, "-c", path, "-o", obj]
         else:
-            cmd = [nvcc] + NVCC_FLAGS + extra + (["-Xptxas", "-v"] if ptxas_info else []) + \
+            cmd = [nvcc] + NVCC_FLAGS + extra + list(extra_nvcc) + (["-Xptxas", "-v"] if ptxas_info else []) + \
                   ["-I" + INCLUDE, "-c", path, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -84,13 +89,13 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
 
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(compile_unit, UNITS))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc, "-shared"] + ARCH + ["-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"linking libairbox.so failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -136,8 +136,10 @@ struct abx_geom {
   std::vector<float> tris_local, xc, dc, zc;
   std::vector<uint8_t> solid, fluid, opening, outlet, cls;
   // device-side, shared by the simulations of this geometry
-  uint32_t *d_mask = nullptr, *d_seg = nullptr;
+  uint32_t *d_mask = nullptr;
+  uint2 *d_seg = nullptr;
   uint32_t nseg = 0;
+  int64_t kpad = 0;
   uint8_t *d_opening = nullptr;
   int64_t *d_cells = nullptr;       // padded index of each fluid cell, compact (c) order
   std::vector<int64_t> cells_p;     // host copy
@@ -338,8 +340,48 @@ static int finish_geometry(abx_geom &g, const abx_prepare_params *p, const std::
 
 // Cell classes of setupSim (src/engine.js:248-255), device mask, fluid
 // segments and the compact cell list.
+static uint2 seg2(uint32_t base, uint32_t lanes) {
+  uint2 v;
+  v.x = base;
+  v.y = lanes;
+  return v;
+}
+
+// The k offset in [0,32) that packs the columns' fluid cells into the fewest
+// 32-cell segments (whole warps of fluid cells in the step kernels).
+static int64_t choose_kpad(const abx_geom &g) {
+  std::vector<int64_t> count(32, 0);
+  const int nz = g.nz;
+  for (int64_t ij = 0; ij < (int64_t)g.nx * g.ny; ij++) {
+    const uint8_t *col = g.fluid.data() + ij * nz;
+    int k = 0;
+    int64_t last[32];
+    for (int t = 0; t < 32; t++) last[t] = -1;
+    while (k < nz) {
+      while (k < nz && !col[k]) k++;
+      if (k >= nz) break;
+      const int a = k;
+      while (k < nz && col[k]) k++;
+      const int b = k - 1;  // fluid run [a, b]
+      for (int t = 0; t < 32; t++) {
+        int64_t s0 = (a + t) / 32, s1 = (b + t) / 32;
+        if (s0 == last[t]) s0++;
+        if (s1 >= s0) count[t] += s1 - s0 + 1;
+        last[t] = s1;
+      }
+    }
+  }
+  int64_t best = 0;
+  for (int t = 1; t < 32; t++) if (count[t] < count[best]) best = t;
+  return best;
+}
+
 static int build_device_geometry(abx_geom &g, cudaStream_t st) {
   const int nx = g.nx, ny = g.ny, nz = g.nz;
+  g.kpad = choose_kpad(g);
+  g.nzp = (g.nz + g.kpad + 31) / 32 * 32;
+  g.Np = (int64_t)g.nx * g.ny * g.nzp;
+  if (19 * g.Np >= (1ll << 32)) return fail(ABX_ERR_INVALID_ARGUMENT, "prepare: grid above 2^32 / 19 padded cells");
   const double dtop = g.dc[g.top];
   g.cls.assign((size_t)g.N, 0);
   g.cells_p.clear();
@@ -360,31 +402,38 @@ static int build_device_geometry(abx_geom &g, cudaStream_t st) {
         else if (g.outlet[c]) cl = 3;
         else if (filt) cl = 4;
         g.cls[c] = cl;
-        g.cells_p.push_back(((int64_t)i * ny + j) * g.nzp + k);
+        g.cells_p.push_back(((int64_t)i * ny + j) * g.nzp + k + g.kpad);
         g.cells_j.push_back(j);
       }
     }
-  // fluid segments: 32-cell runs along k holding any fluid cell
-  std::vector<uint32_t> seg;
-  const int nsegk = (int)(g.nzp / 32);
-  for (int64_t ij = 0; ij < (int64_t)nx * ny; ij++)
-    for (int s = 0; s < nsegk; s++) {
-      const int k0 = 32 * s, k1 = std::min(nz, k0 + 32);
-      bool any = false;
-      for (int k = k0; k < k1 && !any; k++) any = g.cls[ij * nz + k] != 0;
-      if (any) seg.push_back((uint32_t)(ij * g.nzp + k0));
+  // fluid segments: 32-cell runs along k holding any fluid cell, with the lane mask of their fluid cells
+  std::vector<uint2> seg;
+  for (int64_t ij = 0; ij < (int64_t)nx * ny; ij++) {
+    int64_t cur = -1;
+    uint32_t lanes = 0;
+    for (int k = 0; k < nz; k++) {
+      if (!g.cls[ij * nz + k]) continue;
+      const int64_t kk = k + g.kpad, s0 = kk / 32;
+      if (s0 != cur) {
+        if (cur >= 0) seg.push_back(seg2((uint32_t)(ij * g.nzp + cur * 32), lanes));
+        cur = s0;
+        lanes = 0;
+      }
+      lanes |= 1u << (kk % 32);
     }
+    if (cur >= 0) seg.push_back(seg2((uint32_t)(ij * g.nzp + cur * 32), lanes));
+  }
   g.nseg = (uint32_t)seg.size();
   DevBuf dcls;
   CK(cudaMalloc(&dcls.p, (size_t)g.N), "prepare: class array");
   CK(cudaMemcpyAsync(dcls.p, g.cls.data(), (size_t)g.N, cudaMemcpyHostToDevice, st), "prepare: class upload");
-  g.h2d += g.N + (int64_t)(sizeof(uint32_t) * seg.size() + g.opening.size() + sizeof(int64_t) * g.cells_p.size());
+  g.h2d += g.N + (int64_t)(sizeof(uint2) * seg.size() + g.opening.size() + sizeof(int64_t) * g.cells_p.size());
   g.launches += 1;
   CK(cudaMalloc((void **)&g.d_mask, sizeof(uint32_t) * (size_t)g.Np), "prepare: mask");
-  CK(launch_build_mask((const uint8_t *)dcls.p, nx, ny, nz, g.nzp, g.d_mask, st), "prepare: build mask");
-  CK(cudaMalloc((void **)&g.d_seg, sizeof(uint32_t) * std::max<size_t>(seg.size(), 1)), "prepare: segments");
+  CK(launch_build_mask((const uint8_t *)dcls.p, nx, ny, nz, g.nzp, g.kpad, g.d_mask, st), "prepare: build mask");
+  CK(cudaMalloc((void **)&g.d_seg, sizeof(uint2) * std::max<size_t>(seg.size(), 1)), "prepare: segments");
   if (!seg.empty())
-    CK(cudaMemcpyAsync(g.d_seg, seg.data(), sizeof(uint32_t) * seg.size(), cudaMemcpyHostToDevice, st), "prepare: segments");
+    CK(cudaMemcpyAsync(g.d_seg, seg.data(), sizeof(uint2) * seg.size(), cudaMemcpyHostToDevice, st), "prepare: segments");
   CK(cudaMalloc((void **)&g.d_opening, std::max<size_t>(g.opening.size(), 1)), "prepare: opening");
   CK(cudaMemcpyAsync(g.d_opening, g.opening.data(), g.opening.size(), cudaMemcpyHostToDevice, st), "prepare: opening");
   CK(cudaMalloc((void **)&g.d_cells, sizeof(int64_t) * std::max<size_t>(g.cells_p.size(), 1)), "prepare: cells");
@@ -447,7 +496,8 @@ extern "C" int abx_prepare(const float *tris, size_t nfloats, const abx_prepare_
   g.nxf = 3 * g.nx; g.nyf = 3 * g.ny; g.nzf = 3 * g.nz;
   g.nzp = (g.nz + 31) / 32 * 32;
   g.Np = (int64_t)g.nx * g.ny * g.nzp;
-  if (g.Np >= (1ll << 32)) return fail(ABX_ERR_INVALID_ARGUMENT, "prepare: grid above 2^32 padded cells");
+  // the step kernels index populations with 32-bit element offsets
+  if (19 * g.Np >= (1ll << 32)) return fail(ABX_ERR_INVALID_ARGUMENT, "prepare: grid above 2^32 / 19 padded cells");
   g.kf = (int)std::floor((g.mn[2] + 1.5 - g.origin[2]) / hf);
   if (g.kf < 0 || g.kf >= g.nzf) return fail(ABX_ERR_INVALID_ARGUMENT, "prepare: opening slice outside the grid");
   g.xc.resize(g.nx); g.dc.resize(g.ny); g.zc.resize(g.nz);
@@ -879,7 +929,7 @@ extern "C" int abx_sim_evaluate(abx_sim *s, abx_metrics *m, float *fmap, double 
   CK(cudaSetDevice(s->g->device), "sim_evaluate");
   const abx_geom &g = *s->g;
   EvalArgs e{};
-  e.nx = g.nx; e.ny = g.ny; e.nz = g.nz; e.nzp = g.nzp; e.jm = g.jm;
+  e.nx = g.nx; e.ny = g.ny; e.nz = g.nz; e.nzp = g.nzp; e.kpad = g.kpad; e.jm = g.jm;
   e.jb = first_ge(g.dc, g.pleat + 2 * g.h);
   e.nacc = s->nacc; e.u0 = s->u0; e.opening = g.d_opening; e.ns = s->has_ns ? s->d_ns : nullptr;
   e.fmap = s->d_fmap; e.out = s->d_eval;

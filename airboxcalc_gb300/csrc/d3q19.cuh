@@ -35,10 +35,20 @@ constexpr uint32_t kClsBulk = 0, kClsInlet = 1, kClsOutlet = 2, kClsFilter = 3;
 enum StoreKind { kStoreF32 = 0, kStoreF32Exact = 1, kStoreF16 = 2, kStoreBF16 = 3, kStoreF64 = 4 };
 
 template <int K> struct Store;
+// Streaming cache hints (evict-first) for the float32 populations: each value
+// is read once and written once per step.
+#ifndef ABX_CACHE_HINTS
+#define ABX_CACHE_HINTS 1
+#endif
 template <> struct Store<kStoreF32> {
   using T = float; using L = float; using Acc = float;
+#if ABX_CACHE_HINTS
   __device__ static __forceinline__ L ld(const T *p, L) { return __ldcs(p); }
   __device__ static __forceinline__ void st(T *p, L v, L) { __stcs(p, v); }
+#else
+  __device__ static __forceinline__ L ld(const T *p, L) { return *p; }
+  __device__ static __forceinline__ void st(T *p, L v, L) { *p = v; }
+#endif
 };
 template <> struct Store<kStoreF32Exact> {
   using T = float; using L = double; using Acc = float;
@@ -160,6 +170,91 @@ __device__ __forceinline__ void collide(const L (&fi)[19], uint32_t cls, L nsv, 
 #pragma unroll
     for (int q = 0; q < 19; q++) fo[q] = fi[q] - (fi[q] - fe[q]) * it;
   }
+}
+
+// The same collision in float32 with the algebra rearranged for the GPU:
+// moments and the stress tensor from the nine opposite-pair sums s and
+// differences d (f_q +- f_opp(q)), the non-equilibrium stress as
+// Pi(f) - rho/3 I - j u (the second moment of the quadratic equilibrium is
+// exactly rho/3 I + rho u u on D3Q19), and equilibrium plus BGK per opposite
+// pair from a shared even part and an odd part.  Same model as collide();
+// about a third of its arithmetic.
+template <bool HAS_NS>
+__device__ __forceinline__ void collide_fast(const float (&f)[19], uint32_t cls, float nsv_in,
+                                             const CollideParams<float> &P, float (&fo)[19], float &ux, float &uy,
+                                             float &uz, float &rho) {
+  // partial bounce-back acts on bulk and filter cells only (src/engine.js:313-317)
+  const float nsv = (HAS_NS && (cls == kClsBulk || cls == kClsFilter) && nsv_in > 0.0f) ? nsv_in : 0.0f;
+  // opposite pairs: (1,2) x, (3,4) y, (5,6) z, (7,8) +x+y, (9,10) +x-y,
+  // (11,12) +x+z, (13,14) +x-z, (15,16) +y+z, (17,18) +y-z
+  const float s1 = f[1] + f[2], d1 = f[1] - f[2];
+  const float s3 = f[3] + f[4], d3 = f[3] - f[4];
+  const float s5 = f[5] + f[6], d5 = f[5] - f[6];
+  const float s7 = f[7] + f[8], d7 = f[7] - f[8];
+  const float s9 = f[9] + f[10], d9 = f[9] - f[10];
+  const float s11 = f[11] + f[12], d11 = f[11] - f[12];
+  const float s13 = f[13] + f[14], d13 = f[13] - f[14];
+  const float s15 = f[15] + f[16], d15 = f[15] - f[16];
+  const float s17 = f[17] + f[18], d17 = f[17] - f[18];
+  const float sxy = s7 + s9, sxz = s11 + s13, syz = s15 + s17;
+  rho = f[0] + ((s1 + s3) + s5) + ((sxy + sxz) + syz);
+  const float jx = d1 + (d7 + d9) + (d11 + d13);
+  const float jy = d3 + (d7 - d9) + (d15 + d17);
+  const float jz = d5 + (d11 - d13) + (d15 - d17);
+  const float inv = 1.0f / rho;
+  ux = jx * inv; uy = jy * inv; uz = jz * inv;
+  float vx = ux, vy = uy, vz = uz;   // velocity of the equilibrium
+  float r = rho, omega = 1.0f;       // omega = 1: equilibrium overwrite (inlet/outlet)
+  if (cls == kClsInlet) {
+    // Zou/He density from populations with c_z <= 0 (src/engine.js:282-284)
+    const float s0 = f[0] + s1 + s3 + sxy;
+    const float sm = f[6] + f[12] + f[13] + f[16] + f[17];
+    r = rho = (s0 + 2.0f * sm) / (1.0f - P.u0);
+    vx = ux = 0.0f; vy = uy = 0.0f; vz = uz = P.u0;
+  } else if (cls == kClsOutlet) {
+    r = rho = 1.0f;
+  } else {
+    const float r3 = rho * (1.0f / 3.0f);
+    const float nxx = (s1 + sxy + sxz) - r3 - jx * ux;
+    const float nyy = (s3 + sxy + syz) - r3 - jy * uy;
+    const float nzz = (s5 + sxz + syz) - r3 - jz * uz;
+    const float nxy = (s7 - s9) - jx * uy;
+    const float nxz = (s11 - s13) - jx * uz;
+    const float nyz = (s15 - s17) - jy * uz;
+    const float q2 = nxx * nxx + nyy * nyy + nzz * nzz + 2.0f * (nxy * nxy + nxz * nxz + nyz * nyz);
+    const float tau = 0.5f * (P.tau0 + sqrtf(P.tau0 * P.tau0 + P.cs2s * sqrtf(q2) * inv));
+    if (cls == kClsFilter) {
+      const float a1 = tau * P.sig * P.aniso, a2 = tau * P.sig;
+      const float sl = 1.0f - fminf(a1, 0.9f), sv = 1.0f - fminf(a2, 0.9f);
+      vx = ux * sl; vy = uy * sv; vz = uz * sl;
+      ux = 0.5f * (ux + vx); uy = 0.5f * (uy + vy); uz = 0.5f * (uz + vz);
+    }
+    omega = 1.0f / tau;
+  }
+  const float base = 1.0f - 1.5f * (vx * vx + vy * vy + vz * vz);
+  const float w1 = r * (1.0f / 18.0f), w2 = r * (1.0f / 36.0f);
+  const float keep = 1.0f - nsv;
+  // one opposite pair: equilibrium = even +- odd, then relax both
+  auto pair = [&](int q, float cu, float w) {
+    const float even = w * fmaf(4.5f * cu, cu, base), odd = (3.0f * w) * cu;
+    const float ep = even + odd, em = even - odd;
+    const float bp = fmaf(omega, ep - f[q], f[q]), bm = fmaf(omega, em - f[q + 1], f[q + 1]);
+    if (HAS_NS) {
+      fo[q] = keep * bp + nsv * f[q + 1];
+      fo[q + 1] = keep * bm + nsv * f[q];
+    } else {
+      fo[q] = bp; fo[q + 1] = bm;
+    }
+  };
+  {
+    const float e0 = r * (1.0f / 3.0f) * base;
+    const float b0 = fmaf(omega, e0 - f[0], f[0]);
+    fo[0] = HAS_NS ? keep * b0 + nsv * f[0] : b0;
+  }
+  pair(1, vx, w1); pair(3, vy, w1); pair(5, vz, w1);
+  pair(7, vx + vy, w2); pair(9, vx - vy, w2); pair(11, vx + vz, w2);
+  pair(13, vx - vz, w2); pair(15, vy + vz, w2); pair(17, vy - vz, w2);
+  if (HAS_NS) { ux *= keep; uy *= keep; uz *= keep; }
 }
 
 }  // namespace abx

@@ -82,14 +82,15 @@ cudaError_t launch_evaluate(int storage, const StateArgs &a, const EvalArgs &e, 
 // bounds instead of linear wrap-around; the two agree because fluid never
 // touches the grid faces that a wrap could cross (the leak check of
 // src/engine.js:191-195 and the closed last row of :177-178 ensure it).
-__global__ void build_mask_kernel(const uint8_t *cls, int nx, int ny, int nz, int64_t nzp, uint32_t *mask) {
+__global__ void build_mask_kernel(const uint8_t *cls, int nx, int ny, int nz, int64_t nzp, int64_t kpad,
+                                  uint32_t *mask) {
   const int64_t total = (int64_t)nx * ny * nzp;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(p % nzp);
+    const int k = (int)(p % nzp - kpad);
     const int64_t ij = p / nzp;
     const int j = (int)(ij % ny), i = (int)(ij / ny);
     uint32_t m = 0;
-    if (k < nz) {
+    if (k >= 0 && k < nz) {
       const uint8_t c = cls[ij * nz + k];
       if (c) {
 #pragma unroll
@@ -106,9 +107,9 @@ __global__ void build_mask_kernel(const uint8_t *cls, int nx, int ny, int nz, in
   }
 }
 
-cudaError_t launch_build_mask(const uint8_t *cls, int nx, int ny, int nz, int64_t nzp, uint32_t *mask,
+cudaError_t launch_build_mask(const uint8_t *cls, int nx, int ny, int nz, int64_t nzp, int64_t kpad, uint32_t *mask,
                               cudaStream_t st) {
-  build_mask_kernel<<<stride_grid((int64_t)nx * ny * nzp), 256, 0, st>>>(cls, nx, ny, nz, nzp, mask);
+  build_mask_kernel<<<stride_grid((int64_t)nx * ny * nzp), 256, 0, st>>>(cls, nx, ny, nz, nzp, kpad, mask);
   return cudaGetLastError();
 }
 

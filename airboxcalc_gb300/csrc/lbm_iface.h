@@ -3,6 +3,7 @@
 // beyond the runtime's stream type.
 #pragma once
 #include <cuda_runtime_api.h>
+#include <vector_types.h>
 #include <stdint.h>
 
 namespace abx {
@@ -10,7 +11,7 @@ namespace abx {
 struct StepArgs {
   void *f;                 // populations A[19][Np], storage type of the run
   const uint32_t *mask;    // Np cell mask words
-  const uint32_t *seg;     // fluid segment bases (32 cells along k each)
+  const uint2 *seg;        // fluid segments: {base index, bit l set if cell base + l is fluid}
   uint32_t nseg;
   int64_t Np;
   void *acc;               // averages [4][Np] (float, or double for the float64 run)
@@ -42,7 +43,7 @@ struct ProbeArgs {
 
 struct EvalArgs {
   int nx, ny, nz;
-  int64_t nzp;
+  int64_t nzp, kpad;
   int jm, jb, nacc;
   double u0;
   const uint8_t *opening;  // nx*ny
@@ -62,9 +63,10 @@ cudaError_t launch_evaluate(int storage, const StateArgs &a, const EvalArgs &e, 
 // step kernels of the float32-collision storages (lbm_fast.cu)
 cudaError_t launch_step_fast(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, cudaStream_t st);
 
-// Mask construction (mask.cu): class bytes (0 not fluid, 1 bulk, 2 inlet,
-// 3 outlet, 4 filter; index (i*ny+j)*nz+k) -> padded mask words.
-cudaError_t launch_build_mask(const uint8_t *cls, int nx, int ny, int nz, int64_t nzp, uint32_t *mask,
+// Mask construction (lbm_exact.cu): class bytes (0 not fluid, 1 bulk, 2 inlet,
+// 3 outlet, 4 filter; index (i*ny+j)*nz+k) -> padded mask words, cell (i,j,k)
+// at padded index (i*ny+j)*nzp + k + kpad.
+cudaError_t launch_build_mask(const uint8_t *cls, int nx, int ny, int nz, int64_t nzp, int64_t kpad, uint32_t *mask,
                               cudaStream_t st);
 // Scatter compact-order values (ns) to the padded layout.
 cudaError_t launch_scatter_f32(const float *src, const int64_t *cells, int64_t n, float *dst, cudaStream_t st);

@@ -4,11 +4,13 @@
 // float32 storage with cpuStep's float64 collision, and a float64 run).
 //
 // Memory layout in HBM (one simulation):
-//   populations  A[q][p], q = 0..18, p = (i*ny + j)*nzp + k, nzp = nz rounded up to 32
+//   populations  A[q][p], q = 0..18, p = (i*ny + j)*nzp + k + kpad; kpad in [0,32) is
+//                chosen per geometry so that the columns' fluid runs fill whole
+//                32-cell segments, nzp = nz + kpad rounded up to 32
 //                one array only: A-A streaming updates it in place
 //   mask         uint32 per padded cell (see d3q19.cuh)
 //   averages     acc[c][p], c = ux, uy, uz, rho (float32; float64 for the float64 run)
-//   segments     uint32 base index of every 32-cell run along k holding a fluid cell
+//   segments     {base, lane mask} of every 32-cell run along k holding a fluid cell
 //
 // A-A streaming.  The reference pulls f_q(x) = f*_q(x - c_q) from a second
 // array (src/engine.js:272-276, bounce-back from the cell's own opposite
@@ -35,46 +37,66 @@ template <class L> __device__ __forceinline__ CollideParams<L> make_params(const
   return P;
 }
 
+// Tuning knobs (compile-time): minimum resident blocks per SM of the step
+// kernel (0 = let the compiler choose the register count).
+#ifndef ABX_STEP_MINBLOCKS
+#define ABX_STEP_MINBLOCKS 4
+#endif
+
 template <int K, bool ODD, bool ACC, bool HAS_NS>
-__global__ void __launch_bounds__(256) aa_step_kernel(const StepArgs a) {
+__global__ void __launch_bounds__(256, ABX_STEP_MINBLOCKS) aa_step_kernel(const StepArgs a) {
   using S = Store<K>;
   using T = typename S::T;
   using L = typename S::L;
   using Acc = typename S::Acc;
   const uint32_t s = blockIdx.x * 8u + (threadIdx.x >> 5);
   if (s >= a.nseg) return;
-  if (a.status && *(const volatile int *)a.status) return;
-  const int64_t p = (int64_t)a.seg[s] + (threadIdx.x & 31);
-  const uint32_t m = a.mask[p];
-  if (!(m & kFluidBit)) return;
+  // the run-state word changes only between launches: a plain load issued together with the segment's
+  const int halted = a.status ? *a.status : 0;
+  const uint2 sg = a.seg[s];
+  const uint32_t lane = threadIdx.x & 31;
+  if (halted || !((sg.y >> lane) & 1u)) return;
+  // 32-bit element indices: the host guarantees 19 * Np < 2^32
+  const uint32_t p = sg.x + lane;
+  const uint32_t m = a.mask[p];  // in flight together with the population loads below
   T *f = (T *)a.f;
-  const int64_t Np = a.Np;
+  const uint32_t Np = (uint32_t)a.Np;
   L fi[19];
+  if (ODD) {
+    // Pull from the neighbours first.  For a fluid cell x every x - c_q lies
+    // inside the padded array (fluid never touches the grid faces), so the
+    // loads are in bounds even where the neighbour is solid; those
+    // directions are then bounced back from the cell's own slot.
 #pragma unroll
-  for (int q = 0; q < 19; q++) {
-    int64_t idx;
-    if (ODD) idx = ((m >> q) & 1u) ? (int64_t)opp(q) * Np + p - a.off[q] : (int64_t)q * Np + p;
-    else idx = (int64_t)q * Np + p;
-    fi[q] = S::ld(f + idx, weight<L>(q));
+    for (int q = 0; q < 19; q++) fi[q] = S::ld(f + ((uint32_t)opp(q) * Np + p - (uint32_t)a.off[q]), weight<L>(q));
+    if (m != 0x7FFFFu) {
+#pragma unroll
+      for (int q = 1; q < 19; q++)
+        if (!((m >> q) & 1u)) fi[q] = S::ld(f + ((uint32_t)q * Np + p), weight<L>(q));
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < 19; q++) fi[q] = S::ld(f + ((uint32_t)q * Np + p), weight<L>(q));
   }
   const uint32_t cls = (m >> kClassShift) & 3u;
   L nsv = (L)0;
   if (HAS_NS) nsv = (L)a.ns[p];
   L fo[19], ux, uy, uz, rho;
-  collide<L, HAS_NS>(fi, cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
+  if constexpr (sizeof(L) == 4) collide_fast<HAS_NS>(fi, cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
+  else collide<L, HAS_NS>(fi, cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
 #pragma unroll
   for (int q = 0; q < 19; q++) {
-    int64_t idx;
-    if (ODD) idx = ((m >> opp(q)) & 1u) ? (int64_t)q * Np + p + a.off[q] : (int64_t)opp(q) * Np + p;
-    else idx = (int64_t)opp(q) * Np + p;
+    uint32_t idx;
+    if (ODD) idx = ((m >> opp(q)) & 1u) ? (uint32_t)q * Np + p + (uint32_t)a.off[q] : (uint32_t)opp(q) * Np + p;
+    else idx = (uint32_t)opp(q) * Np + p;
     S::st(f + idx, fo[q], weight<L>(q));
   }
   if (ACC) {
     Acc *acc = (Acc *)a.acc;
     acc[p] = (Acc)((L)acc[p] + ux);
     acc[Np + p] = (Acc)((L)acc[Np + p] + uy);
-    acc[2 * Np + p] = (Acc)((L)acc[2 * Np + p] + uz);
-    acc[3 * Np + p] = (Acc)((L)acc[3 * Np + p] + rho);
+    acc[2u * Np + p] = (Acc)((L)acc[2u * Np + p] + uz);
+    acc[3u * Np + p] = (Acc)((L)acc[3u * Np + p] + rho);
   }
 }
 
@@ -251,9 +273,9 @@ __global__ void __launch_bounds__(1024) evaluate_kernel(const StateArgs a, EvalA
   __shared__ double sh[6 * 32];
   const Acc *acc = (const Acc *)a.acc;
   const int nx = e.nx, ny = e.ny, nz = e.nz;
-  const int64_t nzp = e.nzp;
+  const int64_t nzp = e.nzp, kpad = e.kpad;
   const double dn = e.nacc > 1 ? (double)e.nacc : 1.0;
-  auto P = [&](int i, int j, int k) -> int64_t { return ((int64_t)i * ny + j) * nzp + k; };
+  auto P = [&](int i, int j, int k) -> int64_t { return ((int64_t)i * ny + j) * nzp + k + kpad; };
   auto fluid = [&](int64_t p) -> bool {
     if (!(a.mask[p] & kFluidBit)) return false;
     return !(e.ns && e.ns[p] > 0.5f);
