@@ -611,6 +611,7 @@ struct abx_sim {
   void *d_f = nullptr, *d_acc = nullptr;
   float *d_ns = nullptr;
   int *d_status = nullptr;
+  unsigned long long *d_diag = nullptr;
   double *d_hist = nullptr, *d_eval = nullptr;
   float *d_fmap = nullptr;
   int64_t *d_plist = nullptr;
@@ -619,6 +620,8 @@ struct abx_sim {
   int Ain = 0, Af = 0, Lp = 0, nM = 0, nT = 0;
   double u0 = 0, tau0 = 0, sig = 0, aniso = 0, cs2s = 0, uface = 0;
   bool has_ns = false;
+  TmaBlob tma;               // tensor maps of the TMA-pipelined step kernel (tma.ready when in use)
+  bool use_graphs = true;    // ABX_NO_GRAPH=1 launches the step kernels one by one
   std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -630,8 +633,10 @@ struct abx_sim {
   ~abx_sim() {
     cudaSetDevice(g->device);
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    free_tma(&tma);
     for (auto e : ev_pool) cudaEventDestroy(e);
-    cudaFree(d_f); cudaFree(d_acc); cudaFree(d_ns); cudaFree(d_status); cudaFree(d_hist); cudaFree(d_eval);
+    cudaFree(d_f); cudaFree(d_acc); cudaFree(d_ns); cudaFree(d_status); cudaFree(d_diag); cudaFree(d_hist);
+    cudaFree(d_eval);
     cudaFree(d_fmap); cudaFree(d_plist);
     if (st) cudaStreamDestroy(st);
   }
@@ -647,7 +652,7 @@ static void offsets(const abx_geom &g, long long off[19]) {
 static StepArgs step_args(const abx_sim &s) {
   StepArgs a{};
   a.f = s.d_f; a.mask = s.g->d_mask; a.seg = s.g->d_seg; a.nseg = s.g->nseg; a.Np = s.g->Np;
-  a.acc = s.d_acc; a.ns = s.has_ns ? s.d_ns : nullptr; a.status = s.d_status;
+  a.acc = s.d_acc; a.ns = s.has_ns ? s.d_ns : nullptr; a.status = s.d_status; a.diag = s.d_diag;
   offsets(*s.g, a.off);
   a.u0 = s.u0; a.tau0 = s.tau0; a.sig = s.sig; a.aniso = s.aniso; a.cs2s = s.cs2s;
   return a;
@@ -664,6 +669,7 @@ static int sim_reset(abx_sim *s) {
   CK(cudaSetDevice(s->g->device), "sim: set device");
   CK(launch_init(s->p.storage, state_args(*s), s->st), "sim: init");
   CK(cudaMemsetAsync(s->d_status, 0, sizeof(int), s->st), "sim: init");
+  CK(cudaMemsetAsync(s->d_diag, 0, 8 * sizeof(unsigned long long), s->st), "sim: init");
   CK(cudaStreamSynchronize(s->st), "sim: init");
   s->step = 0; s->nacc = 0; s->form = 0; s->nhist = 0;
   s->step_ms = 0; s->step_ms_plain = 0; s->run_ms = 0; s->eval_ms = 0;
@@ -702,6 +708,7 @@ extern "C" int abx_sim_create(abx_geom *g, const abx_run_params *p, const float 
   CK(cudaMalloc(&s.d_f, store_bytes(p->storage) * 19 * (size_t)g->Np), "sim_create: populations");
   CK(cudaMalloc(&s.d_acc, acc_bytes(p->storage) * 4 * (size_t)g->Np), "sim_create: averages");
   CK(cudaMalloc((void **)&s.d_status, sizeof(int)), "sim_create: status");
+  CK(cudaMalloc((void **)&s.d_diag, 8 * sizeof(unsigned long long)), "sim_create: diagnostics");
   s.hist_cap = p->steps / p->every + 2;
   CK(cudaMalloc((void **)&s.d_hist, sizeof(double) * 4 * s.hist_cap), "sim_create: history");
   CK(cudaMalloc((void **)&s.d_eval, sizeof(double) * 16), "sim_create: metrics");
@@ -718,6 +725,16 @@ extern "C" int abx_sim_create(abx_geom *g, const abx_run_params *p, const float 
     CK(cudaMemcpyAsync(tmp.p, ns, sizeof(float) * (size_t)g->nf, cudaMemcpyHostToDevice, s.st), "sim_create: ns");
     CK(launch_scatter_f32((const float *)tmp.p, g->d_cells, g->nf, s.d_ns, s.st), "sim_create: ns");
     CK(cudaStreamSynchronize(s.st), "sim_create: ns");
+  }
+  if (const char *ng = std::getenv("ABX_NO_GRAPH")) s.use_graphs = ng[0] != '1';
+  // TMA-pipelined step kernel for the float32-collision storages, opt-in with ABX_TMA=1 (the direct-load
+  // kernel is the default: it is the faster of the two on GB300)
+  const char *use_tma = std::getenv("ABX_TMA");
+  if ((p->storage == ABX_STORE_F32 || p->storage == ABX_STORE_F16 || p->storage == ABX_STORE_BF16) &&
+      use_tma && use_tma[0] == '1') {
+    cudaError_t te = make_tma(p->storage, step_args(s), &s.tma);
+    if (te != cudaSuccess && te != cudaErrorNotSupported) return cuda_fail(te, "sim_create: tensor maps");
+    cudaGetLastError();
   }
   int rc = sim_reset(&s);
   if (rc) return rc;
@@ -736,6 +753,7 @@ extern "C" int abx_sim_get_info(const abx_sim *s, abx_sim_info *o) {
   o->u0 = s->u0; o->tau0 = s->tau0; o->sig = s->sig; o->aniso = s->aniso; o->cs2s = s->cs2s; o->uface = s->uface;
   o->step = s->step; o->nacc = s->nacc; o->Np = s->g->Np;
   o->state_bytes = (int64_t)(store_bytes(s->p.storage) * 19 + acc_bytes(s->p.storage) * 4) * s->g->Np;
+  o->tma_pipeline = s->tma.ready ? 1 : 0;
   return ABX_OK;
 }
 
@@ -757,6 +775,20 @@ static cudaEvent_t next_event(abx_sim *s) {
 // in "out" form), as one CUDA graph per (n, form, accumulate).
 static int run_steps(abx_sim *s, int n, bool acc) {
   if (n <= 0) return ABX_OK;
+  if (!s->use_graphs) {
+    const StepArgs a = step_args(*s);
+    for (int i = 0; i < n; i++) {
+      CK(launch_step(s->p.storage, s->form == 0, acc, s->has_ns, a, s->tma.ready ? &s->tma : nullptr, s->st), "run: step");
+      s->form ^= 1;
+    }
+    s->step += n;
+    if (acc) s->nacc += n;
+    s->step_launches += n;
+    if (!acc) s->step_launches_plain += n;
+    s->launches += n;
+    s->cell_updates += (int64_t)n * s->g->nf;
+    return ABX_OK;
+  }
   const auto key = std::make_tuple(n, s->form, acc ? 1 : 0);
   auto it = s->graphs.find(key);
   if (it == s->graphs.end()) {
@@ -766,7 +798,7 @@ static int run_steps(abx_sim *s, int n, bool acc) {
     cudaError_t le = cudaSuccess;
     int form = s->form;
     for (int i = 0; i < n && le == cudaSuccess; i++) {
-      le = launch_step(s->p.storage, form == 0, acc, s->has_ns, a, s->st);
+      le = launch_step(s->p.storage, form == 0, acc, s->has_ns, a, s->tma.ready ? &s->tma : nullptr, s->st);
       form ^= 1;
     }
     cudaError_t ce = cudaStreamEndCapture(s->st, &graph);
@@ -813,6 +845,17 @@ static int collect_timing(abx_sim *s) {
   return ABX_OK;
 }
 
+static int pipeline_timeout(abx_sim *s) {
+  unsigned long long d[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  cudaMemcpy(d, s->d_diag, sizeof d, cudaMemcpyDeviceToHost);
+  return fail(ABX_ERR_CUDA,
+              "step kernel: a shared-memory pipeline wait timed out (run halted; block %llu, barrier word %016llx, "
+              "tiles %llu, grid %llu, iteration %llu, tile %llu, armed bytes %llu, smem %llu odd %llu acc %llu, "
+              "segments %llu)",
+              d[1], d[2], d[3] & 0xffffffffull, d[3] >> 32, d[4] & 0xffffffffull, d[4] >> 32, d[5],
+              d[6] & 0xffffffffull, (d[6] >> 32) & 1, (d[6] >> 33) & 1, d[7]);
+}
+
 extern "C" int abx_sim_step(abx_sim *s, int n, int accumulate) {
   if (!s || n < 0) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_step: bad argument");
   CK(cudaSetDevice(s->g->device), "sim_step: set device");
@@ -821,6 +864,10 @@ extern "C" int abx_sim_step(abx_sim *s, int n, int accumulate) {
   rc = collect_timing(s);
   if (rc) return rc;
   CK(cudaStreamSynchronize(s->st), "sim_step: sync");
+  int st = 0;
+  CK(cudaMemcpy(&st, s->d_status, sizeof(int), cudaMemcpyDeviceToHost), "sim_step: status");
+  if (st == -2) return fail(ABX_ERR_CUDA, "step kernel: a TMA copy failed its alignment check (run halted)");
+  if (st < 0) return pipeline_timeout(s);
   return ABX_OK;
 }
 
@@ -828,6 +875,8 @@ static int check_unstable(abx_sim *s) {
   int st = 0;
   CK(cudaMemcpyAsync(&st, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->st), "run: status");
   CK(cudaStreamSynchronize(s->st), "run: status");
+  if (st == -2) return fail(ABX_ERR_CUDA, "step kernel: a TMA copy failed its alignment check (run halted)");
+  if (st < 0) return pipeline_timeout(s);
   if (st)
     return fail(ABX_ERR_UNSTABLE,
                 "Rechnung instabil bei Schritt %d. Zellgröße vergrößern oder Viskosität (tau) erhöhen.", st);

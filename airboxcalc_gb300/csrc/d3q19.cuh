@@ -40,8 +40,11 @@ template <int K> struct Store;
 #ifndef ABX_CACHE_HINTS
 #define ABX_CACHE_HINTS 1
 #endif
+// ld/st address global memory (ld may use global-only cache-hinted loads);
+// lds reads a value staged in shared memory.
 template <> struct Store<kStoreF32> {
   using T = float; using L = float; using Acc = float;
+  __device__ static __forceinline__ L lds(const T *p, L) { return *p; }
 #if ABX_CACHE_HINTS
   __device__ static __forceinline__ L ld(const T *p, L) { return __ldcs(p); }
   __device__ static __forceinline__ void st(T *p, L v, L) { __stcs(p, v); }
@@ -52,21 +55,25 @@ template <> struct Store<kStoreF32> {
 };
 template <> struct Store<kStoreF32Exact> {
   using T = float; using L = double; using Acc = float;
+  __device__ static __forceinline__ L lds(const T *p, L) { return (L)*p; }
   __device__ static __forceinline__ L ld(const T *p, L) { return (L)*p; }
   __device__ static __forceinline__ void st(T *p, L v, L) { *p = (float)v; }
 };
 template <> struct Store<kStoreF16> {
   using T = __half; using L = float; using Acc = float;
+  __device__ static __forceinline__ L lds(const T *p, L w) { return w + __half2float(*p); }
   __device__ static __forceinline__ L ld(const T *p, L w) { return w + __half2float(*p); }
   __device__ static __forceinline__ void st(T *p, L v, L w) { *p = __float2half_rn(v - w); }
 };
 template <> struct Store<kStoreBF16> {
   using T = __nv_bfloat16; using L = float; using Acc = float;
+  __device__ static __forceinline__ L lds(const T *p, L w) { return w + __bfloat162float(*p); }
   __device__ static __forceinline__ L ld(const T *p, L w) { return w + __bfloat162float(*p); }
   __device__ static __forceinline__ void st(T *p, L v, L w) { *p = __float2bfloat16_rn(v - w); }
 };
 template <> struct Store<kStoreF64> {
   using T = double; using L = double; using Acc = double;
+  __device__ static __forceinline__ L lds(const T *p, L) { return *p; }
   __device__ static __forceinline__ L ld(const T *p, L) { return *p; }
   __device__ static __forceinline__ void st(T *p, L v, L) { *p = v; }
 };

@@ -25,11 +25,12 @@ static cudaError_t step_k(bool odd, bool acc, bool has_ns, const StepArgs &a, cu
   return cudaGetLastError();
 }
 
-cudaError_t launch_step(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, cudaStream_t st) {
+cudaError_t launch_step(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, const TmaBlob *tma,
+                        cudaStream_t st) {
   switch (storage) {
     case kStoreF32Exact: return step_k<kStoreF32Exact>(odd, acc, has_ns, a, st);
     case kStoreF64: return step_k<kStoreF64>(odd, acc, has_ns, a, st);
-    case kStoreF32: case kStoreF16: case kStoreBF16: return launch_step_fast(storage, odd, acc, has_ns, a, st);
+    case kStoreF32: case kStoreF16: case kStoreBF16: return launch_step_fast(storage, odd, acc, has_ns, a, tma, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -1,7 +1,18 @@
 // lbm_fast.cu - step kernels with float32 collision: float32 populations (the
 // WGSL lbm_step contract, src/engine.js:378-450) and float16 / bfloat16
 // shifted-deviation storage.  Compiled with the default contraction (FMA).
+// Two forms: the TMA-pipelined persistent kernel (lbm_tma.cuh), used when the
+// tensor maps could be made, and the direct-load kernel (lbm_kernels.cuh).
 #include "lbm_kernels.cuh"
+#include "lbm_tma.cuh"
+
+#include <cudaTypedefs.h>
+
+#include <cstring>
+
+#ifndef ABX_TMA_STAGES
+#define ABX_TMA_STAGES 3
+#endif
 
 namespace abx {
 
@@ -21,7 +32,143 @@ static cudaError_t step_k(bool odd, bool acc, bool has_ns, const StepArgs &a, cu
   return cudaGetLastError();
 }
 
-cudaError_t launch_step_fast(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, cudaStream_t st) {
+// ------------------------------------------------------------------ TMA path
+template <int K, bool O, bool A, bool N>
+static cudaError_t tma_one(const StepArgs &a, const TmaBlob &b, cudaStream_t st) {
+  CUtensorMap m[5];
+  std::memcpy(m, b.maps, sizeof m);
+  aa_step_tma_kernel<K, O, A, N, ABX_TMA_STAGES><<<b.grid, kTmaThreads, TmaStage<K, O, A, N, ABX_TMA_STAGES>::kSmem, st>>>(
+      m[kMapPopEven], m[kMapPopWide], m[kMapPopRow], m[kMapMask], m[kMapAcc], a, b.ntiles);
+  return cudaGetLastError();
+}
+
+template <int K>
+static cudaError_t step_tma(bool odd, bool acc, bool has_ns, const StepArgs &a, const TmaBlob &b, cudaStream_t st) {
+  if (a.nseg == 0) return cudaSuccess;
+  if (odd) {
+    if (acc) return has_ns ? tma_one<K, true, true, true>(a, b, st) : tma_one<K, true, true, false>(a, b, st);
+    return has_ns ? tma_one<K, true, false, true>(a, b, st) : tma_one<K, true, false, false>(a, b, st);
+  }
+  if (acc) return has_ns ? tma_one<K, false, true, true>(a, b, st) : tma_one<K, false, true, false>(a, b, st);
+  return has_ns ? tma_one<K, false, false, true>(a, b, st) : tma_one<K, false, false, false>(a, b, st);
+}
+
+template <int K, bool O, bool A, bool N>
+static cudaError_t tma_attr(int *blocks) {
+  constexpr int smem = TmaStage<K, O, A, N, ABX_TMA_STAGES>::kSmem;
+  auto fn = aa_step_tma_kernel<K, O, A, N, ABX_TMA_STAGES>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  int nb = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kTmaThreads, smem);
+  if (e != cudaSuccess) return e;
+  *blocks = *blocks == 0 ? nb : std::min(*blocks, nb);
+  return cudaSuccess;
+}
+
+template <int K>
+static cudaError_t tma_prepare(int *blocks) {
+  cudaError_t e;
+#define ABX_A(O, A, N) if ((e = tma_attr<K, O, A, N>(blocks)) != cudaSuccess) return e;
+  ABX_A(true, true, true) ABX_A(true, true, false) ABX_A(true, false, true) ABX_A(true, false, false)
+  ABX_A(false, true, true) ABX_A(false, true, false) ABX_A(false, false, true) ABX_A(false, false, false)
+#undef ABX_A
+  return cudaSuccess;
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+cudaError_t make_tma(int storage, const StepArgs &a, TmaBlob *out) {
+  out->ready = false;
+  CUtensorMapDataType dt;
+  int elem, win;
+  switch (storage) {
+    case kStoreF32: dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32; elem = 4; win = TmaGeom<kStoreF32>::kWin; break;
+    case kStoreF16: dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT16; elem = 2; win = TmaGeom<kStoreF16>::kWin; break;
+    case kStoreBF16: dt = CU_TENSOR_MAP_DATA_TYPE_BFLOAT16; elem = 2; win = TmaGeom<kStoreBF16>::kWin; break;
+    default: return cudaErrorNotSupported;
+  }
+  auto enc = encode_fn();
+  if (!enc) return cudaErrorNotSupported;
+  if (a.Np % 32 != 0 || a.Np >= (1ll << 31)) return cudaErrorNotSupported;
+  CUtensorMap maps[5];
+  const cuuint64_t np = (cuuint64_t)a.Np;
+  const cuuint32_t ones[2] = {1, 1};
+  {  // populations, even-step box {32, 19}
+    const cuuint64_t dims[2] = {np, 19}, strides[1] = {np * elem};
+    const cuuint32_t box[2] = {32, 19};
+    if (enc(&maps[0], dt, 2, a.f, dims, strides, box, ones, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
+  for (int m = 1; m <= 2; m++) {  // populations, odd-step rows: {win, 1} for +-z directions, {32, 1} otherwise
+    const cuuint64_t dims[2] = {np, 19}, strides[1] = {np * elem};
+    const cuuint32_t box[2] = {(cuuint32_t)(m == 1 ? win : 32), 1};
+    if (enc(&maps[m], dt, 2, a.f, dims, strides, box, ones, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
+  {  // cell mask words
+    const cuuint64_t dims[1] = {np}, strides[1] = {np * 4};
+    const cuuint32_t box[1] = {32};
+    if (enc(&maps[3], CU_TENSOR_MAP_DATA_TYPE_UINT32, 1, (void *)a.mask, dims, strides, box, ones,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
+  {  // running sums of the averages, box {32, 4}
+    const cuuint64_t dims[2] = {np, 4}, strides[1] = {np * 4};
+    const cuuint32_t box[2] = {32, 4};
+    if (enc(&maps[4], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, a.acc, dims, strides, box, ones,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
+  static_assert(sizeof maps == sizeof out->maps, "five descriptors");
+  std::memcpy(out->maps, maps, sizeof maps);
+  int blocks = 0;
+  cudaError_t e;
+  switch (storage) {
+    case kStoreF32: e = tma_prepare<kStoreF32>(&blocks); break;
+    case kStoreF16: e = tma_prepare<kStoreF16>(&blocks); break;
+    default: e = tma_prepare<kStoreBF16>(&blocks); break;
+  }
+  if (e != cudaSuccess) return e;
+  if (blocks < 1) return cudaErrorNotSupported;
+  int dev = 0, nsm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  out->ntiles = (a.nseg + kTmaSegs - 1) / kTmaSegs;
+  out->grid = std::min<uint32_t>(out->ntiles, (uint32_t)(nsm * blocks));
+  if (out->grid == 0) out->grid = 1;
+  out->ready = true;
+  return cudaSuccess;
+}
+
+void free_tma(TmaBlob *b) { b->ready = false; }
+
+cudaError_t launch_step_fast(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, const TmaBlob *tma,
+                             cudaStream_t st) {
+  if (tma && tma->ready) {
+    switch (storage) {
+      case kStoreF32: return step_tma<kStoreF32>(odd, acc, has_ns, a, *tma, st);
+      case kStoreF16: return step_tma<kStoreF16>(odd, acc, has_ns, a, *tma, st);
+      case kStoreBF16: return step_tma<kStoreBF16>(odd, acc, has_ns, a, *tma, st);
+      default: break;
+    }
+  }
   switch (storage) {
     case kStoreF32: return step_k<kStoreF32>(odd, acc, has_ns, a, st);
     case kStoreF16: return step_k<kStoreF16>(odd, acc, has_ns, a, st);

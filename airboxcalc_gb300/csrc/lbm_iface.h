@@ -17,6 +17,7 @@ struct StepArgs {
   void *acc;               // averages [4][Np] (float, or double for the float64 run)
   const float *ns;         // partial bounce-back per padded cell, or null
   const int *status;       // nonzero once the run went unstable: steps become no-ops
+  unsigned long long *diag;  // 8 words: where a pipeline wait gave up (TMA kernel), or null
   long long off[19];       // pull offset of direction q in the padded layout
   double u0, tau0, sig, aniso, cs2s;
 };
@@ -52,8 +53,23 @@ struct EvalArgs {
   double *out;             // 13 doubles
 };
 
-// Launchers (defined in lbm_fast.cu / lbm_exact.cu).  storage: abx_storage value.
-cudaError_t launch_step(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, cudaStream_t st);
+// TMA descriptors of one simulation: five CUtensorMap (made by make_tma,
+// passed to the kernels by value) and the persistent grid size.
+struct alignas(64) TmaBlob {
+  unsigned char maps[5 * 128];
+  uint32_t ntiles = 0, grid = 0;
+  bool ready = false;
+};
+// Encode the tensor maps of a simulation's arrays and size the persistent
+// grid; returns cudaErrorNotSupported when TMA cannot be used for `storage`.
+// free_tma marks the descriptors unused.
+cudaError_t make_tma(int storage, const StepArgs &a, TmaBlob *out);
+void free_tma(TmaBlob *b);
+
+// Launchers (defined in lbm_fast.cu / lbm_exact.cu).  storage: abx_storage
+// value; tma (may be null) selects the TMA-pipelined kernel.
+cudaError_t launch_step(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, const TmaBlob *tma,
+                        cudaStream_t st);
 cudaError_t launch_init(int storage, const StateArgs &a, cudaStream_t st);
 cudaError_t launch_get_f(int storage, const StateArgs &a, float *out, cudaStream_t st);
 cudaError_t launch_set_f(int storage, const StateArgs &a, const float *in, cudaStream_t st);
@@ -61,7 +77,8 @@ cudaError_t launch_get_acc(int storage, const StateArgs &a, float *out, int nacc
 cudaError_t launch_probe(int storage, const StateArgs &a, const ProbeArgs &p, cudaStream_t st);
 cudaError_t launch_evaluate(int storage, const StateArgs &a, const EvalArgs &e, cudaStream_t st);
 // step kernels of the float32-collision storages (lbm_fast.cu)
-cudaError_t launch_step_fast(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, cudaStream_t st);
+cudaError_t launch_step_fast(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, const TmaBlob *tma,
+                             cudaStream_t st);
 
 // Mask construction (lbm_exact.cu): class bytes (0 not fluid, 1 bulk, 2 inlet,
 // 3 outlet, 4 filter; index (i*ny+j)*nz+k) -> padded mask words, cell (i,j,k)

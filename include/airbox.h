@@ -133,6 +133,7 @@ typedef struct {
   int step, nacc;               /* steps done, steps accumulated */
   int64_t Np;                   /* padded cells held on the device */
   int64_t state_bytes;          /* device bytes of populations + averages */
+  int tma_pipeline;             /* 1 when the step kernel is fed by TMA tensor copies */
 } abx_sim_info;
 int abx_sim_get_info(const abx_sim *s, abx_sim_info *out);
 

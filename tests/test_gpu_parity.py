@@ -214,3 +214,33 @@ def test_prepare_errors_match_reference(name):
         E.prepare({"tris": tris, **p, "maxCells": kw.get("max_cells", 4.5e6)})
     assert eg.value.code == eo.value.code
     assert str(eg.value) == str(eo.value)
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16", "bf16"])
+def test_tma_pipeline_matches_direct_kernel(storage, monkeypatch):
+    """The TMA-fed step kernel and the direct-load kernel run the same
+    collision on the same data: their states agree after odd and even steps,
+    with and without averaging, to float32 rounding (one unit of the stored
+    deviation for the 16-bit formats: the two kernels may contract a
+    multiply-add differently before the value is rounded to 16 bits)."""
+    tol = {"f32": 1e-6, "f16": 1.3e-4, "bf16": 1e-3}[storage]
+    og, g = prep_both(ag.config1_spec())
+    So = O.OracleSim(og, RUN)
+    ns = bulk_ns(So, So.NF)
+    out = {}
+    for tma in (True, False):
+        if tma:
+            monkeypatch.setenv("ABX_TMA", "1")
+        else:
+            monkeypatch.delenv("ABX_TMA", raising=False)
+        for with_ns in (False, True):
+            S = E.Simulation(g, {**RUN, "storage": storage}, ns=ns if with_ns else None)
+            assert S.info.tma_pipeline == (1 if tma else 0)
+            S.step(7)
+            S.step(6, accumulate=True)
+            out[(tma, with_ns)] = (S.get_f(), S.get_acc())
+    for with_ns in (False, True):
+        fa, aa = out[(True, with_ns)]
+        fb, ab = out[(False, with_ns)]
+        assert np.abs(fa - fb).max() < tol
+        assert np.abs(aa - ab).max() < 1e-5
