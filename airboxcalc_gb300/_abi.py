@@ -26,6 +26,7 @@ EXPORTS = [
     "abx_geom_get_info", "abx_geom_get_masks", "abx_geom_get_fine", "abx_sim_create", "abx_sim_free",
     "abx_sim_get_info", "abx_sim_reset", "abx_sim_step", "abx_sim_run", "abx_sim_get_f", "abx_sim_set_f",
     "abx_sim_get_acc", "abx_sim_evaluate", "abx_simulate", "abx_sim_set_timing", "abx_sim_get_timing",
+    "abx_voxelize_static",
 ]
 
 
@@ -123,6 +124,7 @@ def load(build_if_missing: bool = True):
                                C.c_int, C.POINTER(C.c_int)]
     L.abx_sim_set_timing.argtypes = [vp, C.c_int]
     L.abx_sim_get_timing.argtypes = [vp, C.POINTER(Timing)]
+    L.abx_voxelize_static.argtypes = [vp, C.c_size_t, C.c_double * 3, C.c_double, C.c_int, C.c_int, C.c_int, vp, vp]
     _lib = L
     return L
 

@@ -1027,6 +1027,14 @@ extern "C" int abx_simulate(abx_geom *g, const abx_run_params *p, const float *n
   return rc;
 }
 
+extern "C" int abx_voxelize_static(const float *d_tris, size_t nfloats, const double origin[3], double h, int nx,
+                                   int ny, int nz, uint8_t *d_vox, void *stream) {
+  char msg[512] = {0};
+  const int rc = voxelize_static(d_tris, nfloats, origin, h, nx, ny, nz, d_vox, (cudaStream_t)stream, msg, sizeof msg);
+  if (rc) return fail(rc, "%s", msg);
+  return ABX_OK;
+}
+
 extern "C" int abx_sim_set_timing(abx_sim *s, int enabled) {
   if (!s) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_set_timing: null simulation");
   s->timing = enabled != 0;

@@ -107,5 +107,11 @@ struct VoxOut {
 };
 // Runs the whole voxelizer; scratch is allocated and freed inside.
 cudaError_t run_voxelizer(const VoxJob &job, VoxOut &out, cudaStream_t st);
+// The voxelizer on a caller-given grid (nx, ny, nz at cell size h, i.e. the
+// reference's voxelize(T, origin, nx, ny, nz, h)) writing the voxel grid to
+// d_vox, with its scratch in a fixed device array instead of allocations.
+// Returns an abx_status value; msg receives the text of a failure.
+int voxelize_static(const float *d_tris, size_t nfloats, const double origin[3], double h, int nx, int ny, int nz,
+                    uint8_t *d_vox, cudaStream_t st, char *msg, size_t msg_len);
 
 }  // namespace abx

@@ -20,6 +20,9 @@
 // separate kernel writes it for tests.
 #include <math.h>
 #include <stdint.h>
+#include <stdio.h>
+
+#include <mutex>
 
 #include "lbm_iface.h"
 
@@ -331,6 +334,101 @@ done:
   cudaFreeAsync(rec, st); cudaFreeAsync(pre, st); cudaFreeAsync(tmp, st); cudaFreeAsync(cnt, st);
   cudaFreeAsync(cursor, st); cudaFreeAsync(off, st); cudaFreeAsync(nivl, st); cudaFreeAsync(hits, st);
   return rc;
+}
+
+// ------------------------------------------------------------------ voxelizer without device allocation
+// For callers that cannot allocate device memory themselves (see
+// abx_voxelize_static in include/airbox.h).  Same kernels as run_voxelizer;
+// the scratch lives in this fixed device array instead of cudaMallocAsync.
+constexpr size_t kStaticScratchBytes = 32u << 20;   // 32 MiB, held by every GPU that loads the library
+static __device__ __align__(256) unsigned char g_vox_scratch[kStaticScratchBytes];
+
+static std::mutex g_scratch_mu;
+static void *g_scratch_addr[256];   // device address of g_vox_scratch per device ordinal (set once)
+
+static size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+int voxelize_static(const float *d_tris, size_t nfloats, const double origin[3], double h, int nx, int ny, int nz,
+                    uint8_t *d_vox, cudaStream_t st, char *msg, size_t msg_len) {
+  auto err = [&](int code, const char *fmt, long long a, long long b) {
+    snprintf(msg, msg_len, fmt, a, b);
+    return code;
+  };
+  if ((!d_tris && nfloats) || !d_vox || !origin || nx <= 0 || ny <= 0 || nz <= 0 || !(h > 0))
+    return err(20, "voxelize_static: bad argument (%lld, %lld)", (long long)nfloats, (long long)nx);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 256) return err(21, "voxelize_static: no current CUDA device (%lld, %lld)", e, dev);
+  void *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+      // the symbol's name is only a host-side stand-in: resolve its device address
+      // once per device, with that device current
+      e = cudaGetSymbolAddress(&g_scratch_addr[dev], g_vox_scratch);
+      if (e != cudaSuccess) {
+        g_scratch_addr[dev] = nullptr;
+        return err(21, "voxelize_static: cudaGetSymbolAddress failed (error %lld, device %lld)", e, dev);
+      }
+    }
+    base = g_scratch_addr[dev];
+  }
+  const int64_t ncol = (int64_t)nx * ny, ntri = (int64_t)(nfloats / 9);
+  const int64_t tmp_n = (ncol > ntri ? ncol : ntri) / kScanTile + 2;
+  // fixed part of the scratch: triangle records, prefix sums, column counters and offsets
+  size_t o = 0;
+  const size_t o_rec = o;    o += align256(sizeof(TriRec) * (size_t)(ntri > 0 ? ntri : 1));
+  const size_t o_pre = o;    o += align256(sizeof(int64_t) * (size_t)(ntri + 1));
+  const size_t o_tmp = o;    o += align256(sizeof(int64_t) * (size_t)tmp_n);
+  const size_t o_cnt = o;    o += align256(sizeof(uint32_t) * (size_t)ncol);
+  const size_t o_cur = o;    o += align256(sizeof(uint32_t) * (size_t)ncol);
+  const size_t o_off = o;    o += align256(sizeof(int64_t) * (size_t)(ncol + 1));
+  const size_t o_niv = o;    o += align256(sizeof(int) * (size_t)ncol);
+  const size_t o_sli = o;    o += align256((size_t)ncol);
+  const size_t o_hit = o;
+  if (o_hit > kStaticScratchBytes)
+    return err(20, "voxelize_static: this grid and mesh need %lld bytes of scratch before the hits; the library holds %lld",
+               (long long)o_hit, (long long)kStaticScratchBytes);
+  unsigned char *S = (unsigned char *)base;
+  TriRec *rec = (TriRec *)(S + o_rec);
+  int64_t *pre = (int64_t *)(S + o_pre), *tmp = (int64_t *)(S + o_tmp), *off = (int64_t *)(S + o_off);
+  uint32_t *cnt = (uint32_t *)(S + o_cnt), *cursor = (uint32_t *)(S + o_cur);
+  int *nivl = (int *)(S + o_niv);
+  uint8_t *slice = (uint8_t *)(S + o_sli);
+  float *hits = (float *)(S + o_hit);
+  int64_t W = 0, H = 0;
+#define ABX_SC(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return err(21, "voxelize_static: CUDA error %lld at step %lld", e_, __LINE__); } while (0)
+  // the scratch keeps the previous call's contents: zero what the passes accumulate into
+  ABX_SC(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (size_t)ncol, st));
+  ABX_SC(cudaMemsetAsync(cursor, 0, sizeof(uint32_t) * (size_t)ncol, st));
+  if (ntri > 0) {
+    tri_setup_kernel<<<grid_for(ntri), 256, 0, st>>>(d_tris, ntri, origin[0], origin[1], origin[2], h, nx, ny, rec, pre);
+    ABX_SC(cudaGetLastError());
+    ABX_SC(scan_exclusive<int64_t>(pre, ntri, pre, tmp, st));
+    ABX_SC(cudaMemcpyAsync(&W, pre + ntri, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    ABX_SC(cudaStreamSynchronize(st));
+    if (W > 0) {
+      hits_kernel<false><<<grid_for(W), 256, 0, st>>>(rec, pre, ntri, W, h, ny, cnt, nullptr, nullptr, nullptr);
+      ABX_SC(cudaGetLastError());
+    }
+  }
+  ABX_SC(scan_exclusive<uint32_t>(cnt, ncol, off, tmp, st));
+  ABX_SC(cudaMemcpyAsync(&H, off + ncol, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  ABX_SC(cudaStreamSynchronize(st));
+  if (o_hit + sizeof(float) * (size_t)H > kStaticScratchBytes)
+    return err(20, "voxelize_static: %lld surface hits need more scratch than the library holds (%lld bytes)", (long long)H,
+               (long long)kStaticScratchBytes);
+  if (W > 0) {
+    hits_kernel<true><<<grid_for(W), 256, 0, st>>>(rec, pre, ntri, W, h, ny, cnt, off, cursor, hits);
+    ABX_SC(cudaGetLastError());
+  }
+  columns_kernel<<<grid_for(ncol), 256, 0, st>>>(off, ncol, hits, h, nz, 0, nivl, slice);
+  ABX_SC(cudaGetLastError());
+  fine_kernel<<<grid_for(ncol * nz), 256, 0, st>>>(off, hits, nivl, ncol, nz, d_vox);
+  ABX_SC(cudaGetLastError());
+  ABX_SC(cudaStreamSynchronize(st));
+#undef ABX_SC
+  return 0;
 }
 
 }  // namespace abx

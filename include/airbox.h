@@ -200,6 +200,32 @@ typedef struct {
 int abx_sim_set_timing(abx_sim *s, int enabled);
 int abx_sim_get_timing(const abx_sim *s, abx_sim_timing *out);
 
+/* voxelize() without any device allocation.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate GPU memory themselves: a host application
+ * whose memory pool owns every device byte (a framework allocator, a fixed
+ * budget, a process that must not call cudaMalloc while other work is in
+ * flight).  They pass their own device buffers for the input and the output,
+ * and the call uses no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * The parity voxelizer of src/engine.js:45-93 on the grid nx x ny x nz with
+ * cell size h and the given origin: d_tris holds nfloats floats of
+ * local-frame triangles (9 per triangle) in device memory, d_vox receives
+ * nx*ny*nz bytes (index (i*ny + j)*nz + k, 1 = inside) in device memory.
+ * The result is bit-identical to the voxel grid abx_prepare builds (the fine
+ * grid of abx_geom_get_fine when called with 3*nx, 3*ny, 3*nz and h/3).
+ *
+ * Its scratch is a fixed 32 MiB array inside the library, held by every GPU
+ * that loads it until the process exits.  Grids and meshes needing more
+ * scratch are rejected with ABX_ERR_INVALID_ARGUMENT and a message giving the
+ * size.  The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress, with the device current); make that first call
+ * before any stream capture.  All calls share the one array and it keeps the
+ * previous call's contents, so calls that overlap on the GPU (other streams,
+ * other threads) race: issue them one after another.  stream may be NULL. */
+int abx_voxelize_static(const float *d_tris, size_t nfloats, const double origin[3], double h, int nx, int ny, int nz,
+                        uint8_t *d_vox, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
