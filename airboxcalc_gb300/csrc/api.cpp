@@ -615,6 +615,9 @@ struct abx_sim {
   double *d_hist = nullptr, *d_eval = nullptr;
   float *d_fmap = nullptr;
   int64_t *d_plist = nullptr;
+  float *d_probe_vy = nullptr;     // probe scratch: -u_y of every probe cell
+  double *d_probe_part = nullptr;  // probe scratch: per-block partial sums
+  int probe_blocks = 1;
   int hist_cap = 0, nhist = 0;
   int step = 0, nacc = 0, form = 0;
   int Ain = 0, Af = 0, Lp = 0, nM = 0, nT = 0;
@@ -637,7 +640,7 @@ struct abx_sim {
     for (auto e : ev_pool) cudaEventDestroy(e);
     cudaFree(d_f); cudaFree(d_acc); cudaFree(d_ns); cudaFree(d_status); cudaFree(d_diag); cudaFree(d_hist);
     cudaFree(d_eval);
-    cudaFree(d_fmap); cudaFree(d_plist);
+    cudaFree(d_fmap); cudaFree(d_plist); cudaFree(d_probe_vy); cudaFree(d_probe_part);
     if (st) cudaStreamDestroy(st);
   }
 };
@@ -716,6 +719,9 @@ extern "C" int abx_sim_create(abx_geom *g, const abx_run_params *p, const float 
   CK(cudaMalloc((void **)&s.d_plist, sizeof(int64_t) * std::max<size_t>(plist.size(), 1)), "sim_create: probe list");
   if (!plist.empty())
     CK(cudaMemcpyAsync(s.d_plist, plist.data(), sizeof(int64_t) * plist.size(), cudaMemcpyHostToDevice, s.st), "sim_create");
+  s.probe_blocks = (int)std::min<size_t>(std::max<size_t>((plist.size() + kProbeThreads - 1) / kProbeThreads, 1), 152 * 4);
+  CK(cudaMalloc((void **)&s.d_probe_vy, sizeof(float) * std::max<size_t>(plist.size(), 1)), "sim_create: probe scratch");
+  CK(cudaMalloc((void **)&s.d_probe_part, sizeof(double) * 2 * s.probe_blocks), "sim_create: probe scratch");
   if (ns) {
     s.has_ns = true;
     CK(cudaMalloc((void **)&s.d_ns, sizeof(float) * (size_t)g->Np), "sim_create: ns");
@@ -907,10 +913,11 @@ extern "C" int abx_sim_run(abx_sim *s, abx_progress_fn cb, void *user) {
       ProbeArgs pr{};
       pr.plist = s->d_plist; pr.nM = s->nM; pr.nT = s->nT; pr.step = s->step; pr.slot = s->nhist;
       pr.Ain = s->Ain; pr.u0 = s->u0; pr.hist = s->d_hist;
+      pr.vy = s->d_probe_vy; pr.part = s->d_probe_part; pr.nblocks = s->probe_blocks;
       sa.form = s->form;
       CK(launch_probe(s->p.storage, sa, pr, s->st), "sim_run: probe");
       s->nhist++;
-      s->launches++;
+      s->launches += 2;
       if (cb) {
         double h[4];
         CK(cudaMemcpyAsync(h, s->d_hist + 4 * (s->nhist - 1), sizeof h, cudaMemcpyDeviceToHost, s->st), "sim_run: probe");

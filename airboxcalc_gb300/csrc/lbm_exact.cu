@@ -12,7 +12,7 @@ namespace abx {
 template <int K>
 static cudaError_t step_k(bool odd, bool acc, bool has_ns, const StepArgs &a, cudaStream_t st) {
   if (a.nseg == 0) return cudaSuccess;
-  const dim3 grid((a.nseg + 7) / 8), block(256);
+  const dim3 grid((a.nseg + 8 * kStepSpw - 1) / (8 * kStepSpw)), block(256);
 #define ABX_L(O, A, N) aa_step_kernel<K, O, A, N><<<grid, block, 0, st>>>(a)
   if (odd) {
     if (acc) { if (has_ns) ABX_L(true, true, true); else ABX_L(true, true, false); }
@@ -69,7 +69,11 @@ cudaError_t launch_get_acc(int storage, const StateArgs &a, float *out, int nacc
   return cudaGetLastError();
 }
 cudaError_t launch_probe(int storage, const StateArgs &a, const ProbeArgs &p, cudaStream_t st) {
-  ABX_DISPATCH(storage, (probe_kernel<K><<<1, 1024, 0, st>>>(a, p)));
+  if (p.nblocks < 1) return cudaErrorInvalidValue;
+  ABX_DISPATCH(storage, (probe_pass1_kernel<K><<<p.nblocks, kProbeThreads, 0, st>>>(a, p)));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  probe_pass2_kernel<<<1, 1024, 0, st>>>(p, a.status);
   return cudaGetLastError();
 }
 cudaError_t launch_evaluate(int storage, const StateArgs &a, const EvalArgs &e, cudaStream_t st) {

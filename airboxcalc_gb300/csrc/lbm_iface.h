@@ -40,7 +40,11 @@ struct ProbeArgs {
   int step, slot;
   double Ain, u0;
   double *hist;            // 4 doubles per slot: step, gamma, massRatio, outflow
+  float *vy;               // nM + nT floats: the probed -u_y values of one check
+  double *part;            // 2 doubles per block of the first pass
+  int nblocks;             // blocks of the first pass
 };
+constexpr int kProbeThreads = 256;
 
 struct EvalArgs {
   int nx, ny, nz;

@@ -43,60 +43,89 @@ template <class L> __device__ __forceinline__ CollideParams<L> make_params(const
 #define ABX_STEP_MINBLOCKS 4
 #endif
 
+// Segments per warp: with 2, a warp issues the loads of both of its segments
+// before computing either (more bytes in flight per warp).
+#ifndef ABX_STEP_SPW
+#define ABX_STEP_SPW 1
+#endif
+constexpr int kStepSpw = ABX_STEP_SPW;
+
 template <int K, bool ODD, bool ACC, bool HAS_NS>
 __global__ void __launch_bounds__(256, ABX_STEP_MINBLOCKS) aa_step_kernel(const StepArgs a) {
   using S = Store<K>;
   using T = typename S::T;
   using L = typename S::L;
   using Acc = typename S::Acc;
-  const uint32_t s = blockIdx.x * 8u + (threadIdx.x >> 5);
-  if (s >= a.nseg) return;
+  constexpr int SPW = kStepSpw;
+  const uint32_t s0 = (blockIdx.x * 8u + (threadIdx.x >> 5)) * SPW;
+  if (s0 >= a.nseg) return;
   // the run-state word changes only between launches: a plain load issued together with the segment's
   const int halted = a.status ? *a.status : 0;
-  const uint2 sg = a.seg[s];
   const uint32_t lane = threadIdx.x & 31;
-  if (halted || !((sg.y >> lane) & 1u)) return;
-  // 32-bit element indices: the host guarantees 19 * Np < 2^32
-  const uint32_t p = sg.x + lane;
-  const uint32_t m = a.mask[p];  // in flight together with the population loads below
+  uint2 sg[SPW];
+#pragma unroll
+  for (int j = 0; j < SPW; j++) sg[j] = (s0 + j < a.nseg) ? a.seg[s0 + j] : make_uint2(0, 0);
+  if (halted) return;
   T *f = (T *)a.f;
   const uint32_t Np = (uint32_t)a.Np;
-  L fi[19];
-  if (ODD) {
-    // Pull from the neighbours first.  For a fluid cell x every x - c_q lies
-    // inside the padded array (fluid never touches the grid faces), so the
-    // loads are in bounds even where the neighbour is solid; those
-    // directions are then bounced back from the cell's own slot.
+  bool act[SPW];
+  uint32_t p[SPW], m[SPW];
+  L fi[SPW][19];
+  Acc av[SPW][4];
 #pragma unroll
-    for (int q = 0; q < 19; q++) fi[q] = S::ld(f + ((uint32_t)opp(q) * Np + p - (uint32_t)a.off[q]), weight<L>(q));
-    if (m != 0x7FFFFu) {
+  for (int j = 0; j < SPW; j++) {
+    act[j] = (sg[j].y >> lane) & 1u;
+    // 32-bit element indices: the host guarantees 19 * Np < 2^32
+    p[j] = sg[j].x + lane;
+    m[j] = act[j] ? a.mask[p[j]] : 0u;  // in flight together with the population loads below
+    if (!act[j]) continue;
+    if (ODD) {
+      // Pull from the neighbours first.  For a fluid cell x every x - c_q lies
+      // inside the padded array (fluid never touches the grid faces), so the
+      // loads are in bounds even where the neighbour is solid; those
+      // directions are then bounced back from the cell's own slot.
+#pragma unroll
+      for (int q = 0; q < 19; q++)
+        fi[j][q] = S::ld(f + ((uint32_t)opp(q) * Np + p[j] - (uint32_t)a.off[q]), weight<L>(q));
+    } else {
+#pragma unroll
+      for (int q = 0; q < 19; q++) fi[j][q] = S::ld(f + ((uint32_t)q * Np + p[j]), weight<L>(q));
+    }
+    // running sums of the averages: loaded now, in flight with the populations
+    if (ACC) {
+      const Acc *acc = (const Acc *)a.acc;
+      av[j][0] = acc[p[j]]; av[j][1] = acc[Np + p[j]]; av[j][2] = acc[2u * Np + p[j]]; av[j][3] = acc[3u * Np + p[j]];
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < SPW; j++) {
+    if (!act[j]) continue;
+    if (ODD && m[j] != 0x7FFFFu) {
 #pragma unroll
       for (int q = 1; q < 19; q++)
-        if (!((m >> q) & 1u)) fi[q] = S::ld(f + ((uint32_t)q * Np + p), weight<L>(q));
+        if (!((m[j] >> q) & 1u)) fi[j][q] = S::ld(f + ((uint32_t)q * Np + p[j]), weight<L>(q));
     }
-  } else {
+    const uint32_t cls = (m[j] >> kClassShift) & 3u;
+    L nsv = (L)0;
+    if (HAS_NS) nsv = (L)a.ns[p[j]];
+    L fo[19], ux, uy, uz, rho;
+    if constexpr (sizeof(L) == 4) collide_fast<HAS_NS>(fi[j], cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
+    else collide<L, HAS_NS>(fi[j], cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
 #pragma unroll
-    for (int q = 0; q < 19; q++) fi[q] = S::ld(f + ((uint32_t)q * Np + p), weight<L>(q));
-  }
-  const uint32_t cls = (m >> kClassShift) & 3u;
-  L nsv = (L)0;
-  if (HAS_NS) nsv = (L)a.ns[p];
-  L fo[19], ux, uy, uz, rho;
-  if constexpr (sizeof(L) == 4) collide_fast<HAS_NS>(fi, cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
-  else collide<L, HAS_NS>(fi, cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
-#pragma unroll
-  for (int q = 0; q < 19; q++) {
-    uint32_t idx;
-    if (ODD) idx = ((m >> opp(q)) & 1u) ? (uint32_t)q * Np + p + (uint32_t)a.off[q] : (uint32_t)opp(q) * Np + p;
-    else idx = (uint32_t)opp(q) * Np + p;
-    S::st(f + idx, fo[q], weight<L>(q));
-  }
-  if (ACC) {
-    Acc *acc = (Acc *)a.acc;
-    acc[p] = (Acc)((L)acc[p] + ux);
-    acc[Np + p] = (Acc)((L)acc[Np + p] + uy);
-    acc[2u * Np + p] = (Acc)((L)acc[2u * Np + p] + uz);
-    acc[3u * Np + p] = (Acc)((L)acc[3u * Np + p] + rho);
+    for (int q = 0; q < 19; q++) {
+      uint32_t idx;
+      if (ODD)
+        idx = ((m[j] >> opp(q)) & 1u) ? (uint32_t)q * Np + p[j] + (uint32_t)a.off[q] : (uint32_t)opp(q) * Np + p[j];
+      else idx = (uint32_t)opp(q) * Np + p[j];
+      S::st(f + idx, fo[q], weight<L>(q));
+    }
+    if (ACC) {
+      Acc *acc = (Acc *)a.acc;
+      acc[p[j]] = (Acc)((L)av[j][0] + ux);
+      acc[Np + p[j]] = (Acc)((L)av[j][1] + uy);
+      acc[2u * Np + p[j]] = (Acc)((L)av[j][2] + uz);
+      acc[3u * Np + p[j]] = (Acc)((L)av[j][3] + rho);
+    }
   }
 }
 
@@ -223,36 +252,41 @@ __device__ __forceinline__ double block_max(double v, double *sh) {
   return v;
 }
 
-// probeCPU + progressInfo (src/engine.js:324-339) for one progress check:
-// vy = my/r of the post-collision populations on layer jm and layer top+1,
-// gamma, mass ratio, and the instability flag (first non-finite outflow).
-// One block of 1024 threads; two passes so that no scratch is needed.
+// probeCPU + progressInfo (src/engine.js:324-339) for one progress check, in
+// two launches.  First pass (many blocks): vy = my/r of the post-collision
+// populations of every probe cell (layer jm, then layer top+1), stored as
+// float32 like the reference's Float32Array, and per-block sums of -vy over
+// each layer.  Second pass (one block): the fixed-order total, the mean of
+// layer jm, the absolute deviations, gamma, the mass ratio and the
+// instability flag (first non-finite outflow).  Deterministic for a given
+// grid size.
 template <int K>
-__global__ void __launch_bounds__(1024) probe_kernel(const StateArgs a, ProbeArgs pr) {
-  __shared__ double sh[3 * 32];
+__global__ void __launch_bounds__(kProbeThreads) probe_pass1_kernel(const StateArgs a, ProbeArgs pr) {
+  __shared__ double sh[2 * 32];
   const int np = pr.nM + pr.nT;
-  double v[2] = {0.0, 0.0};  // sw, qo
-  for (int n = threadIdx.x; n < np; n += blockDim.x) {
+  double v[2] = {0.0, 0.0};  // sw, qo of this block
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < np; n += gridDim.x * blockDim.x) {
     double f[19];
     read_post_all<K>(a, pr.plist[n], f);
     double r = 0, my = 0;
 #pragma unroll
     for (int q = 0; q < 19; q++) { r += f[q]; my += (double)cy(q) * f[q]; }
     const float vy = (float)(my / r);
+    pr.vy[n] = vy;
     if (n < pr.nM) v[0] += -(double)vy; else v[1] += -(double)vy;
   }
   block_sum<2>(v, sh);
+  if (threadIdx.x == 0) { pr.part[2 * blockIdx.x] = v[0]; pr.part[2 * blockIdx.x + 1] = v[1]; }
+}
+
+static __global__ void __launch_bounds__(1024) probe_pass2_kernel(ProbeArgs pr, int *status) {
+  __shared__ double sh[2 * 32];
+  double v[2] = {0.0, 0.0};
+  for (int b = threadIdx.x; b < pr.nblocks; b += blockDim.x) { v[0] += pr.part[2 * b]; v[1] += pr.part[2 * b + 1]; }
+  block_sum<2>(v, sh);
   const double wm = v[0] / pr.nM, qo = v[1];
   double d[1] = {0.0};
-  for (int n = threadIdx.x; n < pr.nM; n += blockDim.x) {
-    double f[19];
-    read_post_all<K>(a, pr.plist[n], f);
-    double r = 0, my = 0;
-#pragma unroll
-    for (int q = 0; q < 19; q++) { r += f[q]; my += (double)cy(q) * f[q]; }
-    const float vy = (float)(my / r);
-    d[0] += fabs(-(double)vy - wm);
-  }
+  for (int n = threadIdx.x; n < pr.nM; n += blockDim.x) d[0] += fabs(-(double)pr.vy[n] - wm);
   block_sum<1>(d, sh);
   if (threadIdx.x == 0) {
     double *h = pr.hist + 4 * (int64_t)pr.slot;
@@ -260,7 +294,7 @@ __global__ void __launch_bounds__(1024) probe_kernel(const StateArgs a, ProbeArg
     h[1] = 1 - d[0] / (2 * pr.nM * wm);
     h[2] = qo / (pr.Ain * pr.u0);
     h[3] = qo;
-    if (!isfinite(qo) && a.status && *a.status == 0) *(int *)a.status = pr.step;
+    if (!isfinite(qo) && status && *status == 0) *status = pr.step;
   }
 }
 
