@@ -80,6 +80,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     a = ap.parse_args()
+    sys.dont_write_bytecode = True   # leave the reference checkout untouched
     sys.path.insert(0, a.reference)
     import airbox_cfd as R  # the reference's own module
 

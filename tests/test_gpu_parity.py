@@ -244,3 +244,24 @@ def test_tma_pipeline_matches_direct_kernel(storage, monkeypatch):
         fb, ab = out[(False, with_ns)]
         assert np.abs(fa - fb).max() < tol
         assert np.abs(aa - ab).max() < 1e-5
+
+
+@pytest.mark.parametrize("storage", ["f32exact", "f32", "f16"])
+def test_instability_reported_like_the_reference(storage):
+    """progressInfo's check (src/engine.js:334-335): a run that blows up fails
+    with the reference's message; with cpuStep's exact arithmetic at the same
+    step as the oracle."""
+    og, g = prep_both(ag.AirboxSpec(**SMALL))
+    run = dict(K=3.0, aniso=10.0, u=0.45, tau=0.5001, steps=3000, avg=100, every=50)
+    So = O.OracleSim(og, run)
+    with pytest.raises(O.OracleError) as eo:
+        So.simulate(3000, 100, 50, nthreads=NT)
+    S = E.Simulation(g, {**run, "storage": storage})
+    with pytest.raises(E.AirboxError) as eg:
+        S.run()
+    assert eg.value.code == 10 and "Rechnung instabil bei Schritt" in str(eg.value)
+    if storage == "f32exact":
+        assert str(eg.value) == str(eo.value)
+    # the same handle runs again after a reset
+    S.reset()
+    S.step(5)
