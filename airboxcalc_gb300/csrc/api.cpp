@@ -49,6 +49,10 @@ static int cuda_fail(cudaError_t e, const char *what) {
   } while (0)
 
 extern "C" const char *abx_last_error(void) { return g_err.c_str(); }
+
+// A pending error of an earlier, unrelated CUDA call in this process (another
+// library, a destructor) must not be reported as this call's failure.
+static void clear_stale_error() { (void)cudaGetLastError(); }
 extern "C" int abx_abi_version(void) { return ABX_ABI_VERSION; }
 extern "C" int abx_device_count(void) {
   int n = 0;
@@ -445,6 +449,7 @@ static int build_device_geometry(abx_geom &g, cudaStream_t st) {
 }
 
 extern "C" int abx_prepare(const float *tris, size_t nfloats, const abx_prepare_params *p, abx_geom **out) {
+  clear_stale_error();
   if (!p || !out || (!tris && nfloats)) return fail(ABX_ERR_INVALID_ARGUMENT, "prepare: null argument");
   *out = nullptr;
   if (p->seal_axis < 0 || p->seal_axis > 2 || p->inlet_axis < 0 || p->inlet_axis > 2)
@@ -571,6 +576,7 @@ extern "C" int abx_geom_get_masks(const abx_geom *g, uint8_t *solid, uint8_t *fl
 }
 
 extern "C" int abx_geom_get_fine(const abx_geom *g, uint8_t *fine, size_t cap) {
+  clear_stale_error();
   if (!g || !fine) return fail(ABX_ERR_INVALID_ARGUMENT, "geom_get_fine: null argument");
   const int64_t nfine = (int64_t)g->nxf * g->nyf * g->nzf;
   if ((int64_t)cap < nfine) return fail(ABX_ERR_INVALID_ARGUMENT, "geom_get_fine: buffer smaller than nxf*nyf*nzf");
@@ -605,7 +611,8 @@ static size_t store_bytes(int s) {
 static size_t acc_bytes(int s) { return s == ABX_STORE_F64 ? 8 : 4; }
 
 struct abx_sim {
-  abx_geom *g = nullptr;
+  abx_geom *g = nullptr;     // must outlive the run calls; the destructor does not touch it
+  int device = 0;
   abx_run_params p{};
   cudaStream_t st = nullptr;
   void *d_f = nullptr, *d_acc = nullptr;
@@ -634,7 +641,7 @@ struct abx_sim {
   std::vector<int> ev_kind;   // per event pair: 0 plain steps, 1 accumulating steps, 2 run, 3 evaluate
   std::vector<int> ev_nsteps;
   ~abx_sim() {
-    cudaSetDevice(g->device);
+    cudaSetDevice(device);
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
     free_tma(&tma);
     for (auto e : ev_pool) cudaEventDestroy(e);
@@ -683,6 +690,7 @@ static int sim_reset(abx_sim *s) {
 }
 
 extern "C" int abx_sim_create(abx_geom *g, const abx_run_params *p, const float *ns, abx_sim **out) {
+  clear_stale_error();
   if (!out) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_create: null output");
   *out = nullptr;
   if (!g) return fail(ABX_ERR_NOT_PREPARED, "Bitte zuerst die Geometrie prüfen.");
@@ -692,7 +700,7 @@ extern "C" int abx_sim_create(abx_geom *g, const abx_run_params *p, const float 
   if (g->nf <= 0) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_create: geometry has no fluid cells");
   std::unique_ptr<abx_sim> S(new abx_sim());
   abx_sim &s = *S;
-  s.g = g; s.p = *p;
+  s.g = g; s.p = *p; s.device = g->device;
   // setupSim scalars (src/engine.js:246-263)
   s.Ain = g->Ain; s.Lp = g->Lp;
   std::vector<int64_t> plist;
@@ -764,6 +772,7 @@ extern "C" int abx_sim_get_info(const abx_sim *s, abx_sim_info *o) {
 }
 
 extern "C" int abx_sim_reset(abx_sim *s) {
+  clear_stale_error();
   if (!s) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_reset: null simulation");
   return sim_reset(s);
 }
@@ -863,6 +872,7 @@ static int pipeline_timeout(abx_sim *s) {
 }
 
 extern "C" int abx_sim_step(abx_sim *s, int n, int accumulate) {
+  clear_stale_error();
   if (!s || n < 0) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_step: bad argument");
   CK(cudaSetDevice(s->g->device), "sim_step: set device");
   int rc = run_steps(s, n, accumulate != 0);
@@ -892,6 +902,7 @@ static int check_unstable(abx_sim *s) {
 // The step loop of simulate (src/engine.js:346-355): averaging for steps past
 // steps - avg, a progress check at every multiple of `every` and at the end.
 extern "C" int abx_sim_run(abx_sim *s, abx_progress_fn cb, void *user) {
+  clear_stale_error();
   if (!s) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_run: null simulation");
   CK(cudaSetDevice(s->g->device), "sim_run: set device");
   const int steps = s->p.steps, avg = s->p.avg, every = s->p.every;
@@ -941,6 +952,7 @@ extern "C" int abx_sim_run(abx_sim *s, abx_progress_fn cb, void *user) {
 }
 
 extern "C" int abx_sim_get_f(abx_sim *s, float *f) {
+  clear_stale_error();
   if (!s || !f) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_get_f: null argument");
   CK(cudaSetDevice(s->g->device), "sim_get_f");
   DevBuf tmp;
@@ -954,6 +966,7 @@ extern "C" int abx_sim_get_f(abx_sim *s, float *f) {
 }
 
 extern "C" int abx_sim_set_f(abx_sim *s, const float *f) {
+  clear_stale_error();
   if (!s || !f) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_set_f: null argument");
   CK(cudaSetDevice(s->g->device), "sim_set_f");
   DevBuf tmp;
@@ -968,6 +981,7 @@ extern "C" int abx_sim_set_f(abx_sim *s, const float *f) {
 }
 
 extern "C" int abx_sim_get_acc(abx_sim *s, float *acc) {
+  clear_stale_error();
   if (!s || !acc) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_get_acc: null argument");
   CK(cudaSetDevice(s->g->device), "sim_get_acc");
   DevBuf tmp;
@@ -981,6 +995,7 @@ extern "C" int abx_sim_get_acc(abx_sim *s, float *acc) {
 }
 
 extern "C" int abx_sim_evaluate(abx_sim *s, abx_metrics *m, float *fmap, double *hist, int hist_cap, int *nhist) {
+  clear_stale_error();
   if (!s || !m) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_evaluate: null argument");
   CK(cudaSetDevice(s->g->device), "sim_evaluate");
   const abx_geom &g = *s->g;

@@ -192,6 +192,75 @@ def cpu_baseline(spec, run, nthreads: int, target_s: float = 12.0):
     return S.NF * n / el / 1e6, n, el, S.NF
 
 
+# ------------------------------------------------------------------ studies
+KPI = ("gamma", "gammaCore", "lowCore", "maxToMean", "zeta")
+
+
+def solve(g, run, storage, timing=True):
+    """One whole simulate() + evaluate() on the GPU; returns (metrics, averages, device ms)."""
+    from airboxcalc_gb300 import engine as E
+    S = E.Simulation(g, {**run, "storage": storage})
+    S.set_timing(timing)
+    S.run()
+    res = S.evaluate()
+    t = S.timing()
+    return res["metrics"], S.get_acc(), t["run_ms"] + t["eval_ms"], S.NF
+
+
+def study_precision(spec, run, desc):
+    """KPI and field error of every population storage against the float64 run
+    (same airbox, same steps)."""
+    import numpy as np
+    from airboxcalc_gb300 import engine as E
+    g = E.prepare({"tris": __import__("airboxcalc_gb300.airboxgen", fromlist=["x"]).build_airbox(spec),
+                   **spec.prepare_params(), "maxCells": 1e10})
+    ref_m, ref_acc, ref_ms, NF = solve(g, run, "f64")
+    ra = ref_acc.reshape(4, -1).astype(np.float64)
+    rows = []
+    for st in ("f64", "f32exact", "f32", "f16", "bf16"):
+        m, acc, ms, _ = (ref_m, ref_acc, ref_ms, NF) if st == "f64" else solve(g, run, st)
+        a = acc.reshape(4, -1).astype(np.float64)
+        err = {k: (m[k] - ref_m[k]) / abs(ref_m[k]) if ref_m[k] else m[k] - ref_m[k] for k in KPI}
+        l2u = float(np.linalg.norm(a[:3] - ra[:3]) / np.linalg.norm(ra[:3]))
+        l2r = float(np.linalg.norm(a[3] - ra[3]) / np.linalg.norm(ra[3] - 1.0))
+        rows.append({"study": "precision", "workload": desc, "storage": st, "NF": NF,
+                     "steps": run["steps"], "ms": round(ms, 2), "mlups": round(NF * run["steps"] / ms / 1e3, 1),
+                     "kpi": {k: round(m[k], 6) for k in KPI}, "rel_err_vs_f64": {k: float(f"{v:.3e}") for k, v in err.items()},
+                     "rel_l2_u_vs_f64": float(f"{l2u:.3e}"), "rel_l2_rho_minus_1_vs_f64": float(f"{l2r:.3e}")})
+        print(json.dumps(rows[-1]), flush=True)
+    return rows
+
+
+def study_converge(spec, run, desc, storages=("f32", "f16", "bf16"), ladder=(600, 900, 1200, 1500, 2100, 3000, 4500, 6000)):
+    """Steps and device time until gamma core and zeta are within 1 % of the plain
+    float32 run on the full schedule (the reference's fixed 6000/2000 steps).
+    Each ladder entry is a fresh run of S steps averaging the last S/3."""
+    from airboxcalc_gb300 import airboxgen as ag
+    from airboxcalc_gb300 import engine as E
+    g = E.prepare({"tris": ag.build_airbox(spec), **spec.prepare_params(), "maxCells": 1e10})
+    ref_m, _, ref_ms, NF = solve(g, run, "f32")
+    out = []
+    for st in storages:
+        found = None
+        for S_ in ladder:
+            r = dict(run, steps=S_, avg=max(S_ // 3, 1))
+            m, _, ms, _ = solve(g, r, st)
+            dg = abs(m["gammaCore"] - ref_m["gammaCore"]) / abs(ref_m["gammaCore"])
+            dz = abs(m["zeta"] - ref_m["zeta"]) / abs(ref_m["zeta"])
+            if dg < 0.01 and dz < 0.01:
+                found = (S_, ms, dg, dz)
+                break
+        row = {"study": "converge", "workload": desc, "storage": st, "reference_ms": round(ref_ms, 2),
+               "reference_steps": run["steps"],
+               "converged_steps": found[0] if found else None, "converged_ms": round(found[1], 2) if found else None,
+               "err_gammaCore": float(f"{found[2]:.3e}") if found else None,
+               "err_zeta": float(f"{found[3]:.3e}") if found else None,
+               "speedup_vs_reference_schedule": round(ref_ms / found[1], 2) if found else None}
+        out.append(row)
+        print(json.dumps(row), flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -201,9 +270,17 @@ def main():
     ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--study", choices=["precision", "converge"], default=None,
+                    help="instead of the bench line: KPI error per storage vs float64, or steps/time to converged KPIs")
     a = ap.parse_args()
     ws, rank, local = dist_env()
     spec, run, desc = workload(a.workload)
+    if a.study == "precision":
+        study_precision(spec, run, desc)
+        return 0
+    if a.study == "converge":
+        study_converge(spec, run, desc)
+        return 0
 
     if a.impl == "reference":
         if rank != 0:
