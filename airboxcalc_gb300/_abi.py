@@ -25,8 +25,11 @@ EXPORTS = [
     "abx_last_error", "abx_abi_version", "abx_device_count", "abx_parse_stl", "abx_prepare", "abx_geom_free",
     "abx_geom_get_info", "abx_geom_get_masks", "abx_geom_get_fine", "abx_sim_create", "abx_sim_free",
     "abx_sim_get_info", "abx_sim_reset", "abx_sim_step", "abx_sim_run", "abx_sim_get_f", "abx_sim_set_f",
-    "abx_sim_get_acc", "abx_sim_evaluate", "abx_simulate", "abx_sim_set_timing", "abx_sim_get_timing",
+    "abx_sim_get_acc", "abx_sim_clear_acc", "abx_sim_evaluate", "abx_simulate", "abx_sim_set_timing", "abx_sim_get_timing",
     "abx_voxelize_static",
+    "abx_net_create", "abx_net_free", "abx_net_get_info", "abx_net_get_weights", "abx_net_set_weights",
+    "abx_net_add_sample", "abx_net_clear_samples", "abx_net_get_sample", "abx_net_train", "abx_net_eval_loss",
+    "abx_net_forward_backward", "abx_net_predict", "abx_sim_warm_start", "abx_sim_converge", "abx_sim_solve_warm",
 ]
 
 
@@ -83,6 +86,35 @@ class Timing(C.Structure):
                 ("d2h_bytes", C.c_int64)]
 
 
+class NetParams(C.Structure):
+    _fields_ = [("res", C.c_int), ("base", C.c_int), ("levels", C.c_int), ("device", C.c_int),
+                ("seed", C.c_ulonglong)]
+
+
+class NetInfo(C.Structure):
+    _fields_ = [("res", C.c_int), ("base", C.c_int), ("levels", C.c_int), ("in_channels", C.c_int),
+                ("out_channels", C.c_int), ("n_samples", C.c_int), ("n_params", C.c_longlong)]
+
+
+class TrainParams(C.Structure):
+    _fields_ = [("first", C.c_int), ("count", C.c_int), ("epochs", C.c_int), ("batch", C.c_int),
+                ("lr", C.c_double), ("lr_min", C.c_double), ("seed", C.c_ulonglong), ("flip", C.c_int)]
+
+
+class ConvergeParams(C.Structure):
+    _fields_ = [("window", C.c_int), ("min_windows", C.c_int), ("max_steps", C.c_int), ("tol", C.c_double)]
+
+
+class ConvergeResult(C.Structure):
+    _fields_ = [("metrics", Metrics), ("steps", C.c_int), ("windows", C.c_int), ("converged", C.c_int),
+                ("change", C.c_double)]
+
+
+class WarmResult(C.Structure):
+    _fields_ = [("run", ConvergeResult), ("fell_back", C.c_int), ("warm_steps", C.c_int), ("infer_ms", C.c_double),
+                ("total_ms", C.c_double)]
+
+
 _lib = None
 
 
@@ -119,12 +151,29 @@ def load(build_if_missing: bool = True):
     L.abx_sim_get_f.argtypes = [vp, vp]
     L.abx_sim_set_f.argtypes = [vp, vp]
     L.abx_sim_get_acc.argtypes = [vp, vp]
+    L.abx_sim_clear_acc.argtypes = [vp]
     L.abx_sim_evaluate.argtypes = [vp, C.POINTER(Metrics), vp, vp, C.c_int, C.POINTER(C.c_int)]
     L.abx_simulate.argtypes = [vp, C.POINTER(RunParams), vp, PROGRESS_FN, vp, C.POINTER(Metrics), vp, vp,
                                C.c_int, C.POINTER(C.c_int)]
     L.abx_sim_set_timing.argtypes = [vp, C.c_int]
     L.abx_sim_get_timing.argtypes = [vp, C.POINTER(Timing)]
     L.abx_voxelize_static.argtypes = [vp, C.c_size_t, C.c_double * 3, C.c_double, C.c_int, C.c_int, C.c_int, vp, vp]
+    L.abx_net_create.argtypes = [C.POINTER(NetParams), C.POINTER(vp)]
+    L.abx_net_free.argtypes = [vp]
+    L.abx_net_free.restype = None
+    L.abx_net_get_info.argtypes = [vp, C.POINTER(NetInfo)]
+    L.abx_net_get_weights.argtypes = [vp, vp]
+    L.abx_net_set_weights.argtypes = [vp, vp]
+    L.abx_net_add_sample.argtypes = [vp, vp]
+    L.abx_net_clear_samples.argtypes = [vp]
+    L.abx_net_get_sample.argtypes = [vp, C.c_int, vp, vp, vp]
+    L.abx_net_train.argtypes = [vp, C.POINTER(TrainParams), vp]
+    L.abx_net_eval_loss.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.abx_net_forward_backward.argtypes = [vp, vp, vp, vp, C.c_int, C.c_double, vp, vp, C.POINTER(C.c_double)]
+    L.abx_net_predict.argtypes = [vp, vp, vp, vp]
+    L.abx_sim_warm_start.argtypes = [vp, vp]
+    L.abx_sim_converge.argtypes = [vp, C.POINTER(ConvergeParams), C.POINTER(ConvergeResult)]
+    L.abx_sim_solve_warm.argtypes = [vp, vp, C.POINTER(ConvergeParams), C.POINTER(WarmResult)]
     _lib = L
     return L
 

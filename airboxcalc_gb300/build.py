@@ -4,7 +4,10 @@ Translation units, compiled in parallel:
   csrc/voxelize.cu   nvcc, -fmad=false (bit-exact double arithmetic of the parity voxelizer)
   csrc/lbm_exact.cu  nvcc, -fmad=false (cpuStep-exact step, float64 run, probe/evaluate/state kernels)
   csrc/lbm_fast.cu   nvcc (float32 / float16 / bfloat16 step kernels, FMA contraction allowed)
+  csrc/warmstart.cu  nvcc (grid <-> network resampling, warm-start initialisation)
+  csrc/nn.cu         nvcc (layer kernels of the warm-start network, forward and backward)
   csrc/api.cpp       g++ -ffp-contract=off (host side of the C ABI)
+  csrc/net.cpp       g++ (host side of the warm-start network: layers, training loop)
 and linked with nvcc -shared (static CUDA runtime).  No torch, no cmake.
 """
 from __future__ import annotations
@@ -29,7 +32,10 @@ UNITS = [
     ("voxelize.cu", ["-fmad=false"]),
     ("lbm_exact.cu", ["-fmad=false"]),
     ("lbm_fast.cu", []),
+    ("warmstart.cu", []),
+    ("nn.cu", []),
     ("api.cpp", None),
+    ("net.cpp", None),
 ]
 
 

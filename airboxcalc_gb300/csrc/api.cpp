@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "lbm_iface.h"
+#include "net.h"
 
 using namespace abx;
 
@@ -980,6 +981,15 @@ extern "C" int abx_sim_set_f(abx_sim *s, const float *f) {
   return ABX_OK;
 }
 
+extern "C" int abx_sim_clear_acc(abx_sim *s) {
+  clear_stale_error();
+  if (!s) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_clear_acc: null simulation");
+  CK(cudaSetDevice(s->g->device), "sim_clear_acc");
+  CK(cudaMemsetAsync(s->d_acc, 0, acc_bytes(s->p.storage) * 4 * (size_t)s->g->Np, s->st), "sim_clear_acc");
+  s->nacc = 0;
+  return ABX_OK;
+}
+
 extern "C" int abx_sim_get_acc(abx_sim *s, float *acc) {
   clear_stale_error();
   if (!s || !acc) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_get_acc: null argument");
@@ -1070,5 +1080,244 @@ extern "C" int abx_sim_get_timing(const abx_sim *s, abx_sim_timing *o) {
   o->step_ms_plain = s->step_ms_plain; o->step_launches_plain = s->step_launches_plain;
   o->run_ms = s->run_ms; o->eval_ms = s->eval_ms; o->cell_updates = s->cell_updates;
   o->kernel_launches = s->launches; o->h2d_bytes = s->h2d; o->d2h_bytes = s->d2h;
+  return ABX_OK;
+}
+
+// ------------------------------------------------------------------ learned warm start
+struct abx_net {
+  WarmNet net;
+};
+
+static GridDesc grid_desc(const abx_geom &g) {
+  GridDesc d{};
+  d.nx = g.nx; d.ny = g.ny; d.nz = g.nz; d.nzp = g.nzp; d.kpad = g.kpad; d.Np = g.Np; d.mask = g.d_mask;
+  return d;
+}
+
+extern "C" int abx_net_create(const abx_net_params *p, abx_net **out) {
+  clear_stale_error();
+  if (!p || !out) return fail(ABX_ERR_INVALID_ARGUMENT, "net_create: null argument");
+  *out = nullptr;
+  const int R = p->res, L = p->levels;
+  if (R < 8 || R > 256 || (R & (R - 1))) return fail(ABX_ERR_INVALID_ARGUMENT, "net_create: res must be a power of two in [8, 256]");
+  if (L < 1 || L > 6 || (R >> (L - 1)) < 2) return fail(ABX_ERR_INVALID_ARGUMENT, "net_create: levels must be 1..6 with res / 2^(levels-1) >= 2");
+  if (p->base <= 0 || p->base % 8 || (p->base << (L - 1)) > 512) return fail(ABX_ERR_INVALID_ARGUMENT, "net_create: base must be a positive multiple of 8 with base * 2^(levels-1) <= 512");
+  int nd = 0;
+  CK(cudaGetDeviceCount(&nd), "net_create: device count");
+  if (p->device < 0 || p->device >= nd) return fail(ABX_ERR_INVALID_ARGUMENT, "net_create: no device %d", p->device);
+  std::unique_ptr<abx_net> n(new abx_net());
+  n->net.device = p->device;
+  cudaError_t e = n->net.init(R, p->base, L, p->device, p->seed);
+  if (e != cudaSuccess) return cuda_fail(e, "net_create");
+  *out = n.release();
+  return ABX_OK;
+}
+
+extern "C" void abx_net_free(abx_net *n) { delete n; }
+
+extern "C" int abx_net_get_info(const abx_net *n, abx_net_info *o) {
+  if (!n || !o) return fail(ABX_ERR_INVALID_ARGUMENT, "net_get_info: null argument");
+  std::memset(o, 0, sizeof *o);
+  o->res = n->net.R; o->base = n->net.base; o->levels = n->net.levels;
+  o->in_channels = WarmNet::kIn; o->out_channels = WarmNet::kOut;
+  o->n_samples = (int)n->net.samples.size(); o->n_params = n->net.n_params;
+  return ABX_OK;
+}
+
+extern "C" int abx_net_get_weights(abx_net *n, float *w) {
+  clear_stale_error();
+  if (!n || !w) return fail(ABX_ERR_INVALID_ARGUMENT, "net_get_weights: null argument");
+  CK(cudaSetDevice(n->net.device), "net_get_weights");
+  CK(cudaMemcpyAsync(w, n->net.d_p, sizeof(float) * n->net.n_params, cudaMemcpyDeviceToHost, n->net.st), "net_get_weights");
+  CK(cudaStreamSynchronize(n->net.st), "net_get_weights");
+  return ABX_OK;
+}
+
+extern "C" int abx_net_set_weights(abx_net *n, const float *w) {
+  clear_stale_error();
+  if (!n || !w) return fail(ABX_ERR_INVALID_ARGUMENT, "net_set_weights: null argument");
+  for (int64_t i = 0; i < n->net.n_params; i++)
+    if (!std::isfinite(w[i])) return fail(ABX_ERR_INVALID_ARGUMENT, "net_set_weights: weight %lld is not finite", (long long)i);
+  CK(cudaSetDevice(n->net.device), "net_set_weights");
+  CK(cudaMemcpyAsync(n->net.d_p, w, sizeof(float) * n->net.n_params, cudaMemcpyHostToDevice, n->net.st), "net_set_weights");
+  CK(cudaMemsetAsync(n->net.d_m, 0, sizeof(float) * n->net.n_params, n->net.st), "net_set_weights");
+  CK(cudaMemsetAsync(n->net.d_v, 0, sizeof(float) * n->net.n_params, n->net.st), "net_set_weights");
+  n->net.adam_t = 0;
+  CK(cudaStreamSynchronize(n->net.st), "net_set_weights");
+  return ABX_OK;
+}
+
+static int net_sim_check(abx_net *n, abx_sim *s, const char *what) {
+  if (!n || !s) return fail(ABX_ERR_INVALID_ARGUMENT, "%s: null argument", what);
+  if (s->g->device != n->net.device)
+    return fail(ABX_ERR_INVALID_ARGUMENT, "%s: the network lives on device %d, the simulation on device %d", what,
+                n->net.device, s->g->device);
+  return ABX_OK;
+}
+
+extern "C" int abx_net_add_sample(abx_net *n, abx_sim *s) {
+  clear_stale_error();
+  if (int rc = net_sim_check(n, s, "net_add_sample")) return rc;
+  if (s->nacc <= 0) return fail(ABX_ERR_INVALID_ARGUMENT, "net_add_sample: the simulation has no time averages (run it first)");
+  CK(cudaSetDevice(s->g->device), "net_add_sample");
+  CK(cudaStreamSynchronize(s->st), "net_add_sample");
+  cudaError_t e = n->net.add_sample(grid_desc(*s->g), (float)s->p.K, s->p.storage, s->d_acc, s->nacc, s->u0);
+  if (e != cudaSuccess) return cuda_fail(e, "net_add_sample");
+  return ABX_OK;
+}
+
+extern "C" int abx_net_clear_samples(abx_net *n) {
+  if (!n) return fail(ABX_ERR_INVALID_ARGUMENT, "net_clear_samples: null network");
+  n->net.clear_samples();
+  return ABX_OK;
+}
+
+extern "C" int abx_net_get_sample(abx_net *n, int i, float *x, float *t, float *m) {
+  clear_stale_error();
+  if (!n) return fail(ABX_ERR_INVALID_ARGUMENT, "net_get_sample: null network");
+  if (i < 0 || i >= (int)n->net.samples.size()) return fail(ABX_ERR_INVALID_ARGUMENT, "net_get_sample: no sample %d", i);
+  const int64_t V = n->net.voxels();
+  const float *b = n->net.samples[i].buf;
+  CK(cudaSetDevice(n->net.device), "net_get_sample");
+  if (x) CK(cudaMemcpyAsync(x, b, sizeof(float) * WarmNet::kIn * V, cudaMemcpyDeviceToHost, n->net.st), "net_get_sample");
+  if (t) CK(cudaMemcpyAsync(t, b + WarmNet::kIn * V, sizeof(float) * WarmNet::kOut * V, cudaMemcpyDeviceToHost, n->net.st), "net_get_sample");
+  if (m) CK(cudaMemcpyAsync(m, b + (WarmNet::kIn + WarmNet::kOut) * V, sizeof(float) * V, cudaMemcpyDeviceToHost, n->net.st), "net_get_sample");
+  CK(cudaStreamSynchronize(n->net.st), "net_get_sample");
+  return ABX_OK;
+}
+
+extern "C" int abx_net_train(abx_net *n, const abx_train_params *p, double *epoch_loss) {
+  clear_stale_error();
+  if (!n || !p) return fail(ABX_ERR_INVALID_ARGUMENT, "net_train: null argument");
+  const int ns = (int)n->net.samples.size();
+  if (p->first < 0 || p->count <= 0 || p->first + p->count > ns)
+    return fail(ABX_ERR_INVALID_ARGUMENT, "net_train: samples [%d, %d) outside the %d stored", p->first, p->first + p->count, ns);
+  if (p->epochs <= 0 || p->batch <= 0 || p->batch > 1024 || !(p->lr > 0) || !(p->lr_min >= 0))
+    return fail(ABX_ERR_INVALID_ARGUMENT, "net_train: epochs > 0, 0 < batch <= 1024, lr > 0 and lr_min >= 0 required");
+  cudaError_t e = n->net.train(p->first, p->count, p->epochs, p->batch, p->lr, p->lr_min, p->seed, p->flip != 0, epoch_loss);
+  if (e != cudaSuccess) return cuda_fail(e, "net_train");
+  return ABX_OK;
+}
+
+extern "C" int abx_net_eval_loss(abx_net *n, int first, int count, double *loss) {
+  clear_stale_error();
+  if (!n || !loss) return fail(ABX_ERR_INVALID_ARGUMENT, "net_eval_loss: null argument");
+  const int ns = (int)n->net.samples.size();
+  if (first < 0 || count <= 0 || first + count > ns)
+    return fail(ABX_ERR_INVALID_ARGUMENT, "net_eval_loss: samples [%d, %d) outside the %d stored", first, first + count, ns);
+  cudaError_t e = n->net.eval_loss(first, count, loss);
+  if (e != cudaSuccess) return cuda_fail(e, "net_eval_loss");
+  return ABX_OK;
+}
+
+extern "C" int abx_net_forward_backward(abx_net *n, const float *d_x, const float *d_t, const float *d_m, int B,
+                                        double scale, float *d_pred, float *d_grad, double *loss) {
+  clear_stale_error();
+  if (!n || !d_x || !d_t || !d_m || !d_pred || !loss || B <= 0 || B > 1024)
+    return fail(ABX_ERR_INVALID_ARGUMENT, "net_forward_backward: bad argument");
+  WarmNet &w = n->net;
+  CK(cudaSetDevice(w.device), "net_forward_backward");
+  CK(w.ensure_batch(B), "net_forward_backward");
+  const int64_t V = w.voxels();
+  CK(cudaMemcpyAsync(w.input(), d_x, sizeof(float) * B * WarmNet::kIn * V, cudaMemcpyDeviceToDevice, w.st), "net_forward_backward");
+  CK(w.forward(B), "net_forward_backward");
+  CK(w.loss(B, d_t, d_m, scale, d_grad != nullptr, loss), "net_forward_backward");
+  CK(cudaMemcpyAsync(d_pred, w.output(), sizeof(float) * B * WarmNet::kOut * V, cudaMemcpyDeviceToDevice, w.st), "net_forward_backward");
+  if (d_grad) CK(cudaMemcpyAsync(d_grad, w.d_g, sizeof(float) * w.n_params, cudaMemcpyDeviceToDevice, w.st), "net_forward_backward");
+  CK(cudaStreamSynchronize(w.st), "net_forward_backward");
+  return ABX_OK;
+}
+
+// features of s's geometry into the network's input slot 0 and one forward pass
+static int net_infer(abx_net *n, abx_sim *s) {
+  WarmNet &w = n->net;
+  CK(cudaSetDevice(w.device), "net: set device");
+  CK(w.ensure_batch(1), "net: buffers");
+  CK(w.features(grid_desc(*s->g), (float)s->p.K, w.input()), "net: features");
+  CK(w.forward(1), "net: forward");
+  return ABX_OK;
+}
+
+extern "C" int abx_net_predict(abx_net *n, abx_sim *s, float *features, float *pred) {
+  clear_stale_error();
+  if (int rc = net_sim_check(n, s, "net_predict")) return rc;
+  if (int rc = net_infer(n, s)) return rc;
+  WarmNet &w = n->net;
+  const int64_t V = w.voxels();
+  if (features) CK(cudaMemcpyAsync(features, w.input(), sizeof(float) * WarmNet::kIn * V, cudaMemcpyDeviceToHost, w.st), "net_predict");
+  if (pred) CK(cudaMemcpyAsync(pred, w.output(), sizeof(float) * WarmNet::kOut * V, cudaMemcpyDeviceToHost, w.st), "net_predict");
+  CK(cudaStreamSynchronize(w.st), "net_predict");
+  return ABX_OK;
+}
+
+extern "C" int abx_sim_warm_start(abx_sim *s, abx_net *n) {
+  clear_stale_error();
+  if (int rc = net_sim_check(n, s, "sim_warm_start")) return rc;
+  if (int rc = net_infer(n, s)) return rc;
+  WarmNet &w = n->net;
+  CK(cudaStreamSynchronize(w.st), "sim_warm_start");
+  if (int rc = sim_reset(s)) return rc;
+  CK(ws_apply(s->p.storage, state_args(*s), grid_desc(*s->g), w.output(), w.input(), w.R, s->u0, s->st), "sim_warm_start: apply");
+  CK(cudaStreamSynchronize(s->st), "sim_warm_start");
+  s->launches += 1;
+  return ABX_OK;
+}
+
+extern "C" int abx_sim_converge(abx_sim *s, const abx_converge_params *p, abx_converge_result *r) {
+  clear_stale_error();
+  if (!s || !p || !r) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_converge: null argument");
+  if (p->window <= 0 || p->min_windows < 2 || p->max_steps < p->window || !(p->tol > 0))
+    return fail(ABX_ERR_INVALID_ARGUMENT, "sim_converge: window > 0, min_windows >= 2, max_steps >= window and tol > 0 required");
+  CK(cudaSetDevice(s->g->device), "sim_converge");
+  std::memset(r, 0, sizeof *r);
+  r->change = INFINITY;
+  double pg = NAN, pz = NAN;
+  while (r->steps + p->window <= p->max_steps) {
+    CK(cudaMemsetAsync(s->d_acc, 0, acc_bytes(s->p.storage) * 4 * (size_t)s->g->Np, s->st), "sim_converge");
+    s->nacc = 0;
+    if (int rc = run_steps(s, p->window, true)) return rc;
+    abx_metrics m;
+    if (int rc = abx_sim_evaluate(s, &m, nullptr, nullptr, 0, nullptr)) return rc;
+    r->steps += p->window;
+    r->windows++;
+    r->metrics = m;
+    if (!std::isfinite(m.gammaCore) || !std::isfinite(m.zeta))
+      return fail(ABX_ERR_UNSTABLE, "Rechnung instabil bei Schritt %d. Zellgröße vergrößern oder Viskosität (tau) erhöhen.", s->step);
+    if (r->windows >= 2)
+      r->change = std::max(std::fabs(m.gammaCore - pg) / std::fabs(m.gammaCore), std::fabs(m.zeta - pz) / std::fabs(m.zeta));
+    if (r->windows >= p->min_windows && r->change < p->tol) {
+      r->converged = 1;
+      break;
+    }
+    pg = m.gammaCore;
+    pz = m.zeta;
+  }
+  return ABX_OK;
+}
+
+extern "C" int abx_sim_solve_warm(abx_sim *s, abx_net *n, const abx_converge_params *p, abx_warm_result *r) {
+  clear_stale_error();
+  if (!s || !n || !p || !r) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_solve_warm: null argument");
+  std::memset(r, 0, sizeof *r);
+  const auto t0 = std::chrono::steady_clock::now();
+  if (int rc = abx_sim_warm_start(s, n)) return rc;
+  r->infer_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  int rc = abx_sim_converge(s, p, &r->run);
+  r->warm_steps = r->run.steps;
+  if (rc == ABX_ERR_UNSTABLE || (rc == ABX_OK && !r->run.converged)) {
+    // residuals did not fall: the reference's start and schedule
+    r->fell_back = 1;
+    if ((rc = sim_reset(s))) return rc;
+    if ((rc = abx_sim_run(s, nullptr, nullptr))) return rc;
+    abx_metrics m;
+    if ((rc = abx_sim_evaluate(s, &m, nullptr, nullptr, 0, nullptr))) return rc;
+    r->run.metrics = m;
+    r->run.steps = s->p.steps;
+    r->run.windows = 1;
+    r->run.converged = 0;
+  } else if (rc) {
+    return rc;
+  }
+  r->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return ABX_OK;
 }

@@ -118,4 +118,40 @@ cudaError_t run_voxelizer(const VoxJob &job, VoxOut &out, cudaStream_t st);
 int voxelize_static(const float *d_tris, size_t nfloats, const double origin[3], double h, int nx, int ny, int nz,
                     uint8_t *d_vox, cudaStream_t st, char *msg, size_t msg_len);
 
+// ---------------------------------------------------------------- warm start
+// The padded grid as the resampling kernels see it (warmstart.cu).
+struct GridDesc {
+  int nx, ny, nz;
+  int64_t nzp, kpad, Np;
+  const uint32_t *mask;    // nonzero: fluid cell; class in bits 19..20
+};
+// Network input (9 x R^3 floats), with two R^3 int scratch arrays for the jump flood.
+cudaError_t ws_features(const GridDesc &g, int R, float K, float *out, int *seed_a, int *seed_b, cudaStream_t st);
+// Training target (4 x R^3) and loss weight (R^3) from a run's averages.
+cudaError_t ws_targets(const GridDesc &g, int storage, const void *acc, int nacc, double u0, int R, float *t, float *m,
+                       cudaStream_t st);
+// Equilibrium populations of the predicted field (4 x R^3) on every fluid cell, "out" form.
+cudaError_t ws_apply(int storage, const StateArgs &a, const GridDesc &g, const float *pred, const float *fluid, int R,
+                     double u0, cudaStream_t st);
+// Mirror one sample's C x R^3 block along x, negating channel neg (< 0: none).
+cudaError_t ws_flip_x(float *t, int C, int R, int neg, cudaStream_t st);
+
+// Layer kernels of the network (nn.cu), float32 [B][C][D][H][W].
+cudaError_t nn_conv3d(const float *x, const float *w, const float *b, float *y, int B, int Cin, int Cout, int D,
+                      int H, int W, int s, int relu, int accum, cudaStream_t st);
+// ReLU adjoint applied to dy in place (relu != 0), then dx (+)= data gradient (dx may be null), dw, db;
+// part: scratch of at least nn_wgrad_scratch_floats(Cin, Cout, output voxels) floats.
+cudaError_t nn_conv3d_backward(const float *x, const float *w, const float *y, float *dy, float *dx, float *dw,
+                               float *db, float *part, int64_t part_floats, int B, int Cin, int Cout, int D, int H,
+                               int W, int s, int relu, int accum_dx, cudaStream_t st);
+int64_t nn_wgrad_scratch_floats(int Cin, int Cout, int Vo);
+cudaError_t nn_upsample2(const float *x, float *y, int64_t BC, int D, int H, int W, cudaStream_t st);
+cudaError_t nn_upsample2_backward(const float *dy, float *dx, int64_t BC, int D, int H, int W, int accum,
+                                  cudaStream_t st);
+cudaError_t nn_axpy(float *y, const float *x, float a, int64_t n, cudaStream_t st);
+cudaError_t nn_mse(const float *pred, const float *target, const float *mask, float *grad, double *part, int nparts,
+                   int B, int C, int64_t V, double scale, cudaStream_t st);
+cudaError_t nn_adam(float *p, const float *g, float *m, float *v, int64_t n, float lr, float b1, float b2, float eps,
+                    int t, cudaStream_t st);
+
 }  // namespace abx

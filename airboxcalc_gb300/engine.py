@@ -242,6 +242,10 @@ class Simulation:
         assert f.size == 19 * self.NF
         _check(A.load().abx_sim_set_f(self._h, _ptr(f)))
 
+    def clear_acc(self):
+        """Start a new averaging window (populations kept)."""
+        _check(A.load().abx_sim_clear_acc(self._h))
+
     def get_acc(self) -> np.ndarray:
         a = np.empty(4 * self.NF, np.float32)
         _check(A.load().abx_sim_get_acc(self._h, _ptr(a)))

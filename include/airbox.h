@@ -162,6 +162,11 @@ int abx_sim_run(abx_sim *s, abx_progress_fn cb, void *user);
  * layout, and the way back (for self-tests and warm starts). */
 int abx_sim_get_f(abx_sim *s, float *f);
 int abx_sim_set_f(abx_sim *s, const float *f);
+/* Clears the time averages (sums and step count) and keeps the populations:
+ * the next accumulating steps start a new averaging window.  No counterpart
+ * in the reference (its averaging window is fixed by steps/avg); used by the
+ * windowed convergence run. */
+int abx_sim_clear_acc(abx_sim *s);
 /* Time-averaged fields acc[comp*NF + a], comp = ux, uy, uz, rho, divided by
  * the accumulated step count as simulate() does (src/engine.js:356). */
 int abx_sim_get_acc(abx_sim *s, float *acc);
@@ -225,6 +230,107 @@ int abx_sim_get_timing(const abx_sim *s, abx_sim_timing *out);
  * other threads) race: issue them one after another.  stream may be NULL. */
 int abx_voxelize_static(const float *d_tris, size_t nfloats, const double origin[3], double h, int nx, int ny, int nz,
                         uint8_t *d_vox, void *stream);
+
+/* ======================================================================
+ * Learned warm start and windowed convergence.  No counterpart in the
+ * reference: engine.js always starts from f = w_i (src/engine.js:261) and
+ * runs the fixed steps/avg schedule.
+ *
+ * The network is a 3-D convolutional encoder-decoder on an R^3 resampling
+ * of the grid (levels L, channels base << l).  Input: fluid / inlet /
+ * outlet / filter fraction of each voxel's footprint, wall distance, K and
+ * the grid extent; output: the time-averaged u / u0 and (rho - 1)/(15 u0^2).
+ * Training, inference, the resampling and the equilibrium initialisation
+ * all run in the library's CUDA kernels on the network's device.
+ * ====================================================================== */
+typedef struct abx_net abx_net;
+
+typedef struct {
+  int res;                  /* R, a power of two >= 8, divisible by 2^(levels-1) */
+  int base;                 /* channels of level 0 (a multiple of 8) */
+  int levels;               /* encoder levels, 1..6 */
+  int device;
+  unsigned long long seed;  /* weight initialisation */
+} abx_net_params;
+
+typedef struct {
+  int res, base, levels, in_channels, out_channels, n_samples;
+  long long n_params;
+} abx_net_info;
+
+int abx_net_create(const abx_net_params *p, abx_net **out);
+void abx_net_free(abx_net *n);
+int abx_net_get_info(const abx_net *n, abx_net_info *out);
+/* All weights and biases, n_params floats (layer by layer, weights
+ * [cout][cin][3][3][3] then biases). */
+int abx_net_get_weights(abx_net *n, float *w);
+int abx_net_set_weights(abx_net *n, const float *w);
+
+/* Training set, kept on the device: adds the features of s's geometry and K
+ * and, as the target, s's current time averages (after abx_sim_run). */
+int abx_net_add_sample(abx_net *n, abx_sim *s);
+int abx_net_clear_samples(abx_net *n);
+/* Read back stored sample i: x (in_channels*R^3), t (4*R^3), m (R^3); any may be NULL. */
+int abx_net_get_sample(abx_net *n, int i, float *x, float *t, float *m);
+
+typedef struct {
+  int first, count;         /* samples [first, first+count) */
+  int epochs, batch;
+  double lr, lr_min;        /* Adam; rate decays from lr to lr_min (cosine) over the call, with a linear
+                               warm-up over the network's first 100 updates */
+  unsigned long long seed;  /* shuffling and mirror augmentation */
+  int flip;                 /* nonzero: mirror half the samples along x */
+} abx_train_params;
+/* epoch_loss: `epochs` doubles (mean weighted MSE per epoch), may be NULL. */
+int abx_net_train(abx_net *n, const abx_train_params *p, double *epoch_loss);
+int abx_net_eval_loss(abx_net *n, int first, int count, double *loss);
+
+/* One forward (and backward) pass on caller device buffers, for checks:
+ * d_x (B*in_channels*R^3), d_t (B*4*R^3), d_m (B*R^3); writes the prediction
+ * to d_pred (B*4*R^3) and, when d_grad is not NULL, the gradient of
+ * loss = scale * sum m (pred - t)^2 w.r.t. the parameters to d_grad. */
+int abx_net_forward_backward(abx_net *n, const float *d_x, const float *d_t, const float *d_m, int B, double scale,
+                             float *d_pred, float *d_grad, double *loss);
+
+/* Network input for s's geometry (in_channels*R^3 floats, host) and the
+ * prediction (4*R^3, host); either may be NULL. */
+int abx_net_predict(abx_net *n, abx_sim *s, float *features, float *pred);
+
+/* Warm start: f = feq(rho, u) of the prediction, interpolated to every fluid
+ * cell (weighted by voxel fluid fraction, |u| <= 0.2, 0.9 <= rho <= 1.1);
+ * averages and step count cleared. */
+int abx_sim_warm_start(abx_sim *s, abx_net *n);
+
+typedef struct {
+  int window;               /* steps per averaging window */
+  int min_windows;          /* windows before the stop rule may fire (>= 2) */
+  int max_steps;            /* give up after this many steps */
+  double tol;               /* stop when gamma core and zeta of two consecutive windows agree within tol (relative) */
+} abx_converge_params;
+
+typedef struct {
+  abx_metrics metrics;      /* evaluate() of the last window's averages */
+  int steps, windows, converged;
+  double change;            /* last window-to-window relative change */
+} abx_converge_result;
+
+/* Windowed run from the current state: averaging windows of `window` steps
+ * until the stop rule fires or max_steps.  Non-finite KPIs end the run with
+ * ABX_ERR_UNSTABLE. */
+int abx_sim_converge(abx_sim *s, const abx_converge_params *p, abx_converge_result *r);
+
+typedef struct {
+  abx_converge_result run;  /* the windowed run (or the plain run after a fallback) */
+  int fell_back;            /* 1: the warm-started run did not converge; re-run from f = w_i on the full schedule */
+  int warm_steps;           /* steps of the warm-started attempt */
+  double infer_ms;          /* features + network + equilibrium initialisation */
+  double total_ms;          /* wall time of the whole call */
+} abx_warm_result;
+
+/* Warm start, windowed run, and the fallback: when the warm-started run does
+ * not converge within max_steps (or goes unstable) the simulation is reset to
+ * f = w_i and runs the reference's steps/avg schedule (abx_sim_run). */
+int abx_sim_solve_warm(abx_sim *s, abx_net *n, const abx_converge_params *p, abx_warm_result *r);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,172 @@
+"""The learned warm start on the GPU, through the C ABI:
+
+* the network's forward pass, loss and parameter gradients (hand-written CUDA
+  kernels) against torch's CPU conv3d autograd in float64;
+* the resampling kernels (features, targets) and the warm-start
+  initialisation against the numpy restatement in oracle/warmstart_ref.py;
+* training lowers the loss; the windowed convergence run and its fallback
+  to the reference's schedule (which must then give exactly the plain run's
+  KPIs).
+"""
+import numpy as np
+import pytest
+
+from airboxcalc_gb300 import airboxgen as ag
+from airboxcalc_gb300 import engine as E
+from airboxcalc_gb300 import warmstart as W
+from oracle import warmstart_ref as R_
+
+pytestmark = pytest.mark.gpu
+
+SMALL = dict(Lx=130.37, Ly=95.29, Lz=110.53, t=3.11, d_in=40.3, stub=21.7, pleat=40.0, dx=5.0,
+             baffle={"z": 50.19, "x0": 3.11, "x1": 60.07, "y0": 70.21})
+RUN = dict(K=3, aniso=10, u=0.06, tau=0.51, steps=60, avg=20, every=30)
+
+
+def geometry(spec=None):
+    spec = spec or ag.AirboxSpec(**SMALL)
+    return E.prepare({"tris": ag.build_airbox(spec), **spec.prepare_params()})
+
+
+def _torch():
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    return torch
+
+
+@pytest.mark.parametrize("res,base,levels", [(8, 8, 2), (16, 8, 3)])
+def test_network_gradients_match_torch_autograd(res, base, levels):
+    torch = _torch()
+    net = W.Net(res, base, levels, seed=3)
+    w = net.get_weights()
+    assert w.size == net.n_params
+    rng = np.random.default_rng(1)
+    B = 2
+    x = rng.standard_normal((B, 9, res, res, res)).astype(np.float32)
+    t = rng.standard_normal((B, 4, res, res, res)).astype(np.float32)
+    m = rng.uniform(0, 1, (B, res, res, res)).astype(np.float32)
+    scale = 1.0 / (4 * float(m.sum()))
+    dx, dt, dm = (torch.from_numpy(a).cuda() for a in (x, t, m))
+    dpred = torch.empty((B, 4, res, res, res), dtype=torch.float32, device="cuda")
+    dgrad = torch.empty(net.n_params, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    loss = net.forward_backward(dx.data_ptr(), dt.data_ptr(), dm.data_ptr(), B, scale, dpred.data_ptr(),
+                                dgrad.data_ptr())
+    pred, grad = dpred.cpu().numpy(), dgrad.cpu().numpy()
+
+    layers = R_.unpack(w, base, levels, torch)
+    X, T, M = (torch.tensor(a, dtype=torch.float64) for a in (x, t, m))
+    P = R_.net_forward(layers, X, levels, torch)
+    L = scale * (M[:, None] * (P - T) ** 2).sum()
+    L.backward()
+    ref_pred = P.detach().numpy()
+    assert np.abs(pred - ref_pred).max() <= 1e-4 * np.abs(ref_pred).max()
+    assert abs(loss - L.item()) <= 1e-5 * abs(L.item())
+    off = 0
+    for i, (wt, bs, s, relu) in enumerate(layers):
+        for ref in (wt.grad.numpy().ravel(), bs.grad.numpy().ravel()):
+            got = grad[off:off + ref.size]
+            off += ref.size
+            err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
+            assert err < 1e-4, f"layer {i}: relative gradient error {err:.2e}"
+    assert off == grad.size
+
+
+def test_features_and_targets_match_restatement():
+    g = geometry()
+    net = W.Net(16, 8, 2)
+    S = E.Simulation(g, RUN)
+    S.run()
+    net.add_sample(S)
+    x, t, m = net.sample(0)
+    fx, _ = net.predict(S)
+    assert np.array_equal(x, fx)
+    cls = R_.classes(g)
+    rx, dist = R_.features(cls, 16, RUN["K"])
+    for c in (0, 1, 2, 3, 5, 6, 7, 8):
+        assert np.array_equal(x[c], rx[c]), f"feature channel {c}"
+    assert (cls == 2).any() and (cls == 4).any()
+    # jump flooding against the exact distance transform
+    d = np.abs(x[4] - rx[4])
+    assert (d < 1e-6).mean() > 0.97 and d.max() < 0.1
+    # targets: footprint means of the time-averaged fields
+    acc = S.get_acc().reshape(4, -1)
+    fl = g.fluid.reshape(g.nx, g.ny, g.nz).astype(bool)
+    avg = {}
+    for c, k in enumerate(("ux", "uy", "uz", "rho")):
+        a = np.zeros((g.nx, g.ny, g.nz))
+        a[fl] = acc[c]
+        avg[k] = a
+    rt, rm = R_.targets(cls, avg, 16, RUN["u"])
+    assert np.allclose(m, rm, rtol=0, atol=1e-6)
+    assert np.abs(t - rt).max() < 2e-4 * max(1.0, np.abs(rt).max())
+
+
+@pytest.mark.parametrize("storage,tol", [("f32", 2e-6), ("f32exact", 2e-6), ("f16", 2e-4), ("bf16", 2e-3)])
+def test_warm_start_populations_match_restatement(storage, tol):
+    g = geometry()
+    net = W.Net(16, 8, 2, seed=7)
+    # make the prediction non-trivial: scale the head so |u| reaches a few u0
+    w = net.get_weights()
+    w[-(4 * 8 * 27 + 4):] *= 20.0
+    net.set_weights(w)
+    S = E.Simulation(g, dict(RUN, storage=storage))
+    feats, pred = net.predict(S)
+    W.warm_start(S, net)
+    f = S.get_f().reshape(19, -1)
+    ijk = np.argwhere(g.fluid.reshape(g.nx, g.ny, g.nz))
+    ref = R_.apply(pred.astype(np.float64), feats[0].astype(np.float64), ijk, (g.nx, g.ny, g.nz), RUN["u"])
+    assert np.abs(f - ref).max() < tol
+    assert np.abs(ref[0] - 1 / 3).max() > 1e-4          # the start differs from f = w_i
+    assert S.refresh().step == 0 and S.info.nacc == 0
+
+
+def test_training_lowers_the_loss():
+    _torch()
+    net = W.Net(16, 8, 2, seed=11)
+    for s in (3, 4, 5):
+        spec = ag.random_spec(s, dx=4.0)
+        g = geometry(spec)
+        S = E.Simulation(g, dict(RUN, steps=200, avg=100, every=100))
+        S.run()
+        net.add_sample(S)
+    assert net.info["n_samples"] == 3
+    before = net.eval_loss(0, 3)
+    hist = net.train(0, 3, 60, batch=2, lr=3e-3, lr_min=1e-4, seed=1, flip=True)
+    after = net.eval_loss(0, 3)
+    assert np.all(np.isfinite(hist))
+    assert after < 0.3 * before, (before, after, hist[-5:])
+
+
+def test_converge_and_fallback_to_the_reference_schedule():
+    g = geometry()
+    net = W.Net(16, 8, 2, seed=5)
+    S = E.Simulation(g, RUN)
+    W.warm_start(S, net)
+    r = W.converge(S, window=20, min_windows=2, max_steps=400, tol=0.5)
+    assert r["converged"] and r["steps"] % 20 == 0 and r["windows"] >= 2
+    assert all(np.isfinite(v) for v in r["metrics"].values())
+    # a stop rule that cannot fire: the run falls back to f = w_i and the full schedule
+    S2 = E.Simulation(g, RUN)
+    res = W.solve_warm(S2, net, window=20, min_windows=2, max_steps=40, tol=1e-14)
+    assert res["fell_back"] and res["warm_steps"] == 40 and res["steps"] == RUN["steps"]
+    plain = E.simulate(g, RUN)["metrics"]
+    for k in ("gamma", "gammaCore", "zeta", "maxToMean"):
+        assert res["metrics"][k] == plain[k], k
+    assert res["total_ms"] >= res["infer_ms"] > 0
+
+
+def test_net_argument_errors():
+    with pytest.raises(E.AirboxError):
+        W.Net(12, 8, 2)            # not a power of two
+    with pytest.raises(E.AirboxError):
+        W.Net(16, 12, 2)           # base not a multiple of 8
+    with pytest.raises(E.AirboxError):
+        W.Net(8, 8, 4)             # 8 / 2^3 < 2
+    net = W.Net(8, 8, 2)
+    g = geometry()
+    S = E.Simulation(g, RUN)
+    with pytest.raises(E.AirboxError):
+        net.add_sample(S)          # no averages yet
+    with pytest.raises(E.AirboxError):
+        net.train(0, 1, 1)         # no samples
