@@ -30,6 +30,8 @@ EXPORTS = [
     "abx_net_create", "abx_net_free", "abx_net_get_info", "abx_net_get_weights", "abx_net_set_weights",
     "abx_net_add_sample", "abx_net_clear_samples", "abx_net_get_sample", "abx_net_train", "abx_net_eval_loss",
     "abx_net_forward_backward", "abx_net_predict", "abx_sim_warm_start", "abx_sim_converge", "abx_sim_solve_warm",
+    "abx_batch_create", "abx_batch_free", "abx_batch_sim", "abx_batch_tune", "abx_batch_set_shape", "abx_batch_reset",
+    "abx_batch_run", "abx_batch_get_info", "abx_sim_field3d", "abx_sim_planes", "abx_sim_streamlines",
 ]
 
 
@@ -102,7 +104,8 @@ class TrainParams(C.Structure):
 
 
 class ConvergeParams(C.Structure):
-    _fields_ = [("window", C.c_int), ("min_windows", C.c_int), ("max_steps", C.c_int), ("tol", C.c_double)]
+    _fields_ = [("settle", C.c_int), ("window", C.c_int), ("min_avg", C.c_int), ("max_steps", C.c_int),
+                ("tol", C.c_double)]
 
 
 class ConvergeResult(C.Structure):
@@ -113,6 +116,32 @@ class ConvergeResult(C.Structure):
 class WarmResult(C.Structure):
     _fields_ = [("run", ConvergeResult), ("fell_back", C.c_int), ("warm_steps", C.c_int), ("infer_ms", C.c_double),
                 ("total_ms", C.c_double)]
+
+
+class Field3DInfo(C.Structure):
+    _fields_ = [(k, C.c_int) for k in ("nx", "ny", "nz", "kB", "jm", "top")] + \
+               [(k, C.c_double) for k in ("h", "x0", "d0", "z0", "zIn", "pleat", "pin", "rho_ref")]
+
+
+class PlanesInfo(C.Structure):
+    _fields_ = [(k, C.c_int) for k in ("ic", "jc", "jlow", "n1", "n2", "lon_n1", "lon_n2")] + \
+               [(k, C.c_double) for k in ("depth_inlet", "depth_low", "x_lon")]
+
+
+class LinesInfo(C.Structure):
+    _fields_ = [(k, C.c_int) for k in ("seeds_opening", "seeds_traced", "n_lines", "n_points")]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("shape", C.c_int), ("spw", C.c_int), ("min_blocks", C.c_int), ("grid", C.c_uint),
+                ("ntiles", C.c_uint), ("ms_per_step", C.c_double), ("n_candidates", C.c_int),
+                ("cand_shape", C.c_int * 32), ("cand_grid", C.c_uint * 32), ("cand_ms", C.c_double * 32)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("n", C.c_int), ("cells", C.c_longlong), ("state_bytes", C.c_longlong), ("ntiles1", C.c_uint),
+                ("ntiles2", C.c_uint), ("shape", C.c_int), ("grid", C.c_uint), ("run_ms", C.c_double),
+                ("kernel_launches", C.c_longlong)]
 
 
 _lib = None
@@ -174,6 +203,18 @@ def load(build_if_missing: bool = True):
     L.abx_sim_warm_start.argtypes = [vp, vp]
     L.abx_sim_converge.argtypes = [vp, C.POINTER(ConvergeParams), C.POINTER(ConvergeResult)]
     L.abx_sim_solve_warm.argtypes = [vp, vp, C.POINTER(ConvergeParams), C.POINTER(WarmResult)]
+    L.abx_sim_field3d.argtypes = [vp, vp, vp, vp, C.POINTER(Field3DInfo)]
+    L.abx_sim_planes.argtypes = [vp, vp, C.POINTER(PlanesInfo)]
+    L.abx_sim_streamlines.argtypes = [vp, C.c_int, vp, vp, vp, C.c_size_t, C.c_size_t, C.POINTER(LinesInfo)]
+    L.abx_batch_create.argtypes = [C.POINTER(vp), C.POINTER(RunParams), C.c_int, C.POINTER(vp)]
+    L.abx_batch_free.argtypes = [vp]
+    L.abx_batch_free.restype = None
+    L.abx_batch_sim.argtypes = [vp, C.c_int, C.POINTER(vp)]
+    L.abx_batch_tune.argtypes = [vp, C.POINTER(BatchTuning)]
+    L.abx_batch_set_shape.argtypes = [vp, C.c_int, C.c_uint]
+    L.abx_batch_reset.argtypes = [vp]
+    L.abx_batch_run.argtypes = [vp, vp]
+    L.abx_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
     _lib = L
     return L
 

@@ -6,6 +6,7 @@ Translation units, compiled in parallel:
   csrc/lbm_fast.cu   nvcc (float32 / float16 / bfloat16 step kernels, FMA contraction allowed)
   csrc/warmstart.cu  nvcc (grid <-> network resampling, warm-start initialisation)
   csrc/nn.cu         nvcc (layer kernels of the warm-start network, forward and backward)
+  csrc/postproc.cu   nvcc, -fmad=false (field3d, cut planes, streamlines in the reference's float64 order)
   csrc/api.cpp       g++ -ffp-contract=off (host side of the C ABI)
   csrc/net.cpp       g++ (host side of the warm-start network: layers, training loop)
 and linked with nvcc -shared (static CUDA runtime).  No torch, no cmake.
@@ -34,6 +35,7 @@ UNITS = [
     ("lbm_fast.cu", []),
     ("warmstart.cu", []),
     ("nn.cu", []),
+    ("postproc.cu", ["-fmad=false"]),
     ("api.cpp", None),
     ("net.cpp", None),
 ]

@@ -128,6 +128,11 @@ struct Frame {
     L[1] = -sd * (q[dAx] - seal);
     L[2] = -sy * a + cy * b;
   }
+  void model(double X, double D, double Z, double q[3]) const {  // makeFrame.toModel (src/engine.js:40)
+    q[oAx] = cy * X - sy * Z;
+    q[dAx] = seal - sd * D;
+    q[iAx] = -si * (sy * X + cy * Z);
+  }
 };
 
 struct abx_geom {
@@ -1266,15 +1271,20 @@ extern "C" int abx_sim_warm_start(abx_sim *s, abx_net *n) {
 extern "C" int abx_sim_converge(abx_sim *s, const abx_converge_params *p, abx_converge_result *r) {
   clear_stale_error();
   if (!s || !p || !r) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_converge: null argument");
-  if (p->window <= 0 || p->min_windows < 2 || p->max_steps < p->window || !(p->tol > 0))
-    return fail(ABX_ERR_INVALID_ARGUMENT, "sim_converge: window > 0, min_windows >= 2, max_steps >= window and tol > 0 required");
+  if (p->settle < 0 || p->window <= 0 || p->min_avg < p->window || p->max_steps < p->settle + p->window || !(p->tol > 0))
+    return fail(ABX_ERR_INVALID_ARGUMENT,
+                "sim_converge: settle >= 0, window > 0, min_avg >= window, max_steps >= settle + window and tol > 0 required");
   CK(cudaSetDevice(s->g->device), "sim_converge");
   std::memset(r, 0, sizeof *r);
   r->change = INFINITY;
+  if (p->settle > 0) {
+    if (int rc = run_steps(s, p->settle, false)) return rc;
+    r->steps = p->settle;
+  }
+  CK(cudaMemsetAsync(s->d_acc, 0, acc_bytes(s->p.storage) * 4 * (size_t)s->g->Np, s->st), "sim_converge");
+  s->nacc = 0;
   double pg = NAN, pz = NAN;
   while (r->steps + p->window <= p->max_steps) {
-    CK(cudaMemsetAsync(s->d_acc, 0, acc_bytes(s->p.storage) * 4 * (size_t)s->g->Np, s->st), "sim_converge");
-    s->nacc = 0;
     if (int rc = run_steps(s, p->window, true)) return rc;
     abx_metrics m;
     if (int rc = abx_sim_evaluate(s, &m, nullptr, nullptr, 0, nullptr)) return rc;
@@ -1285,7 +1295,7 @@ extern "C" int abx_sim_converge(abx_sim *s, const abx_converge_params *p, abx_co
       return fail(ABX_ERR_UNSTABLE, "Rechnung instabil bei Schritt %d. Zellgröße vergrößern oder Viskosität (tau) erhöhen.", s->step);
     if (r->windows >= 2)
       r->change = std::max(std::fabs(m.gammaCore - pg) / std::fabs(m.gammaCore), std::fabs(m.zeta - pz) / std::fabs(m.zeta));
-    if (r->windows >= p->min_windows && r->change < p->tol) {
+    if (s->nacc >= p->min_avg && r->change < p->tol) {
       r->converged = 1;
       break;
     }
@@ -1319,5 +1329,405 @@ extern "C" int abx_sim_solve_warm(abx_sim *s, abx_net *n, const abx_converge_par
     return rc;
   }
   r->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return ABX_OK;
+}
+
+// ------------------------------------------------------------------ batched variants
+struct abx_batch {
+  int device = 0, n = 0;
+  std::vector<abx_sim *> sims;       // owned
+  int storage = 0, steps = 0, avg = 0, every = 1;
+  cudaStream_t st = nullptr;
+  StepArgs *d_vars = nullptr;
+  uint2 *d_tiles[2] = {nullptr, nullptr};   // tiles of 8 (spw 1) and 16 (spw 2) segments
+  uint32_t ntiles[2] = {0, 0};
+  int shape = 0;
+  uint32_t grid = 0;
+  int step = 0, form = 0, nacc = 0;
+  std::map<std::tuple<int, int, int, int, uint32_t>, cudaGraphExec_t> graphs;  // (n, form, acc, shape, grid)
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  double run_ms = 0;
+  int64_t launches = 0;
+  ~abx_batch() {
+    cudaSetDevice(device);
+    if (st) cudaStreamSynchronize(st);
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    for (auto e : ev) if (e) cudaEventDestroy(e);
+    cudaFree(d_vars); cudaFree(d_tiles[0]); cudaFree(d_tiles[1]);
+    for (auto *s : sims) delete s;
+    if (st) cudaStreamDestroy(st);
+  }
+  uint32_t tiles_of(int sh) const { return ntiles[batch_shape_spw(sh) - 1]; }
+  const uint2 *tile_ptr(int sh) const { return d_tiles[batch_shape_spw(sh) - 1]; }
+};
+
+extern "C" int abx_batch_create(abx_geom *const *geoms, const abx_run_params *params, int n, abx_batch **out) {
+  clear_stale_error();
+  if (!geoms || !params || !out || n <= 0) return fail(ABX_ERR_INVALID_ARGUMENT, "batch_create: bad argument");
+  *out = nullptr;
+  const abx_run_params &p0 = params[0];
+  if (p0.storage != ABX_STORE_F32 && p0.storage != ABX_STORE_F16 && p0.storage != ABX_STORE_BF16)
+    return fail(ABX_ERR_INVALID_ARGUMENT, "batch_create: batches run float32, float16 or bfloat16 storage");
+  for (int i = 0; i < n; i++) {
+    if (!geoms[i]) return fail(ABX_ERR_NOT_PREPARED, "batch_create: variant %d has no geometry", i);
+    if (geoms[i]->device != geoms[0]->device) return fail(ABX_ERR_INVALID_ARGUMENT, "batch_create: variants on different devices");
+    const abx_run_params &p = params[i];
+    if (p.storage != p0.storage || p.steps != p0.steps || p.avg != p0.avg || p.every != p0.every)
+      return fail(ABX_ERR_INVALID_ARGUMENT, "batch_create: variant %d differs in storage, steps, avg or every", i);
+  }
+  std::unique_ptr<abx_batch> B(new abx_batch());
+  abx_batch &b = *B;
+  b.device = geoms[0]->device; b.n = n;
+  b.storage = p0.storage; b.steps = p0.steps; b.avg = p0.avg; b.every = p0.every;
+  b.sims.reserve(n);
+  for (int i = 0; i < n; i++) {
+    abx_sim *s = nullptr;
+    if (int rc = abx_sim_create(geoms[i], &params[i], nullptr, &s)) return rc;
+    free_tma(&s->tma);  // batched steps use the tile-list kernel
+    b.sims.push_back(s);
+  }
+  CK(cudaSetDevice(b.device), "batch_create");
+  CK(cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking), "batch_create: stream");
+  CK(cudaEventCreate(&b.ev[0]), "batch_create: events");
+  CK(cudaEventCreate(&b.ev[1]), "batch_create: events");
+  std::vector<StepArgs> vars(n);
+  std::vector<uint2> tiles[2];
+  for (int i = 0; i < n; i++) {
+    vars[i] = step_args(*b.sims[i]);
+    const uint32_t nseg = b.sims[i]->g->nseg;
+    for (int k = 0; k < 2; k++)
+      for (uint32_t s0 = 0; s0 < nseg; s0 += 8u * (k + 1)) tiles[k].push_back(seg2((unsigned)i, s0));
+  }
+  CK(cudaMalloc((void **)&b.d_vars, sizeof(StepArgs) * n), "batch_create: variants");
+  CK(cudaMemcpyAsync(b.d_vars, vars.data(), sizeof(StepArgs) * n, cudaMemcpyHostToDevice, b.st), "batch_create");
+  for (int k = 0; k < 2; k++) {
+    b.ntiles[k] = (uint32_t)tiles[k].size();
+    CK(cudaMalloc((void **)&b.d_tiles[k], sizeof(uint2) * std::max<size_t>(tiles[k].size(), 1)), "batch_create: tiles");
+    if (!tiles[k].empty())
+      CK(cudaMemcpyAsync(b.d_tiles[k], tiles[k].data(), sizeof(uint2) * tiles[k].size(), cudaMemcpyHostToDevice, b.st), "batch_create");
+  }
+  CK(cudaStreamSynchronize(b.st), "batch_create");
+  b.shape = 0;
+  b.grid = std::max<uint32_t>(b.tiles_of(0), 1);
+  *out = B.release();
+  return ABX_OK;
+}
+
+extern "C" void abx_batch_free(abx_batch *b) { delete b; }
+
+extern "C" int abx_batch_sim(abx_batch *b, int i, abx_sim **out) {
+  if (!b || !out || i < 0 || i >= b->n) return fail(ABX_ERR_INVALID_ARGUMENT, "batch_sim: no variant %d", i);
+  *out = b->sims[i];
+  return ABX_OK;
+}
+
+static int batch_sync_state(abx_batch *b) {
+  for (auto *s : b->sims) { s->step = b->step; s->form = b->form; s->nacc = b->nacc; }
+  return ABX_OK;
+}
+
+extern "C" int abx_batch_reset(abx_batch *b) {
+  clear_stale_error();
+  if (!b) return fail(ABX_ERR_INVALID_ARGUMENT, "batch_reset: null batch");
+  CK(cudaSetDevice(b->device), "batch_reset");
+  CK(cudaStreamSynchronize(b->st), "batch_reset");
+  for (auto *s : b->sims)
+    if (int rc = sim_reset(s)) return rc;
+  b->step = 0; b->form = 0; b->nacc = 0;
+  return ABX_OK;
+}
+
+// n batched steps from the current form, one CUDA graph per (n, form, acc, shape, grid)
+static int batch_steps(abx_batch *b, int n, bool acc) {
+  if (n <= 0) return ABX_OK;
+  const auto key = std::make_tuple(n, b->form, acc ? 1 : 0, b->shape, b->grid);
+  auto it = b->graphs.find(key);
+  if (it == b->graphs.end()) {
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal), "batch: capture");
+    cudaError_t le = cudaSuccess;
+    int form = b->form;
+    for (int i = 0; i < n && le == cudaSuccess; i++) {
+      le = launch_step_batch(b->storage, form == 0, acc, b->shape, b->d_vars, b->tile_ptr(b->shape), b->tiles_of(b->shape),
+                             b->grid, b->st);
+      form ^= 1;
+    }
+    cudaError_t ce = cudaStreamEndCapture(b->st, &graph);
+    if (le != cudaSuccess) { if (ce == cudaSuccess) cudaGraphDestroy(graph); return cuda_fail(le, "batch: step launch"); }
+    CK(ce, "batch: capture");
+    cudaGraphExec_t exec;
+    cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ie, "batch: graph instantiate");
+    it = b->graphs.emplace(key, exec).first;
+  }
+  CK(cudaGraphLaunch(it->second, b->st), "batch: graph launch");
+  b->form ^= (n & 1);
+  b->step += n;
+  if (acc) b->nacc += n;
+  b->launches += n;
+  return ABX_OK;
+}
+
+extern "C" int abx_batch_set_shape(abx_batch *b, int shape, unsigned grid) {
+  if (!b || shape < 0 || shape >= kBatchShapes || grid == 0)
+    return fail(ABX_ERR_INVALID_ARGUMENT, "batch_set_shape: shape 0..%d and grid > 0 required", kBatchShapes - 1);
+  b->shape = shape;
+  b->grid = std::min<uint32_t>(grid, std::max<uint32_t>(b->tiles_of(shape), 1));
+  return ABX_OK;
+}
+
+extern "C" int abx_batch_tune(abx_batch *b, abx_batch_tuning *out) {
+  clear_stale_error();
+  if (!b || !out) return fail(ABX_ERR_INVALID_ARGUMENT, "batch_tune: null argument");
+  CK(cudaSetDevice(b->device), "batch_tune");
+  std::memset(out, 0, sizeof *out);
+  if (int rc = abx_batch_reset(b)) return rc;
+  int nsm = 0;
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->device), "batch_tune");
+  constexpr int kReps = 6;  // odd+even step pairs timed per candidate
+  double best = INFINITY;
+  int best_shape = 0;
+  uint32_t best_grid = 1;
+  for (int sh = 0; sh < kBatchShapes; sh++) {
+    const uint32_t nt = b->tiles_of(sh);
+    if (nt == 0) continue;
+    const uint32_t mb = (uint32_t)batch_shape_minblocks(sh);
+    const uint32_t grids[4] = {nt, (uint32_t)nsm * mb, (uint32_t)nsm * mb * 2, (uint32_t)nsm * mb * 4};
+    for (int gi = 0; gi < 4; gi++) {
+      const uint32_t grid = std::min(grids[gi], nt);
+      bool dup = false;
+      for (int c = 0; c < out->n_candidates; c++) dup |= out->cand_shape[c] == sh && out->cand_grid[c] == grid;
+      if (dup || out->n_candidates >= 32) continue;
+      for (int w = 0; w < 2; w++)
+        CK(launch_step_batch(b->storage, (w & 1) == 0, false, sh, b->d_vars, b->tile_ptr(sh), nt, grid, b->st), "batch_tune");
+      CK(cudaEventRecord(b->ev[0], b->st), "batch_tune");
+      for (int r = 0; r < 2 * kReps; r++)
+        CK(launch_step_batch(b->storage, (r & 1) == 0, false, sh, b->d_vars, b->tile_ptr(sh), nt, grid, b->st), "batch_tune");
+      CK(cudaEventRecord(b->ev[1], b->st), "batch_tune");
+      CK(cudaEventSynchronize(b->ev[1]), "batch_tune");
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]), "batch_tune");
+      const double per = ms / (2.0 * kReps);
+      const int c = out->n_candidates++;
+      out->cand_shape[c] = sh; out->cand_grid[c] = grid; out->cand_ms[c] = per;
+      if (per < best) { best = per; best_shape = sh; best_grid = grid; }
+    }
+  }
+  b->shape = best_shape;
+  b->grid = best_grid;
+  out->shape = best_shape; out->spw = batch_shape_spw(best_shape); out->min_blocks = batch_shape_minblocks(best_shape);
+  out->grid = best_grid; out->ntiles = b->tiles_of(best_shape); out->ms_per_step = best;
+  return abx_batch_reset(b);   // the tuning steps advanced the state: start over from f = w_i
+}
+
+extern "C" int abx_batch_run(abx_batch *b, int *status) {
+  clear_stale_error();
+  if (!b) return fail(ABX_ERR_INVALID_ARGUMENT, "batch_run: null batch");
+  CK(cudaSetDevice(b->device), "batch_run");
+  const int start_acc = b->steps - b->avg;
+  b->launches = 0;
+  CK(cudaEventRecord(b->ev[0], b->st), "batch_run");
+  while (b->step < b->steps) {
+    int stop = (b->step / b->every + 1) * b->every;
+    if (stop > b->steps) stop = b->steps;
+    if (b->step < start_acc && stop > start_acc) stop = start_acc;
+    const bool acc = b->step >= start_acc;
+    if (int rc = batch_steps(b, stop - b->step, acc)) return rc;
+    if (b->step % b->every == 0 || b->step == b->steps) {
+      batch_sync_state(b);
+      for (auto *s : b->sims) {
+        if (s->nhist >= s->hist_cap) return fail(ABX_ERR_INVALID_ARGUMENT, "batch_run: history full (reset the batch)");
+        ProbeArgs pr{};
+        pr.plist = s->d_plist; pr.nM = s->nM; pr.nT = s->nT; pr.step = s->step; pr.slot = s->nhist;
+        pr.Ain = s->Ain; pr.u0 = s->u0; pr.hist = s->d_hist;
+        pr.vy = s->d_probe_vy; pr.part = s->d_probe_part; pr.nblocks = s->probe_blocks;
+        CK(launch_probe(s->p.storage, state_args(*s), pr, b->st), "batch_run: probe");
+        s->nhist++;
+        b->launches += 2;
+      }
+    }
+  }
+  CK(cudaEventRecord(b->ev[1], b->st), "batch_run");
+  CK(cudaEventSynchronize(b->ev[1]), "batch_run");
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]), "batch_run");
+  b->run_ms = ms;
+  batch_sync_state(b);
+  for (int i = 0; i < b->n; i++) {
+    abx_sim *s = b->sims[i];
+    s->cell_updates += (int64_t)s->step * s->g->nf;
+    if (status) {
+      int v = 0;
+      CK(cudaMemcpy(&v, s->d_status, sizeof(int), cudaMemcpyDeviceToHost), "batch_run: status");
+      status[i] = v > 0 ? v : 0;
+      if (v < 0) return fail(ABX_ERR_CUDA, "batch_run: variant %d: step kernel halted (%d)", i, v);
+    }
+  }
+  return ABX_OK;
+}
+
+extern "C" int abx_batch_get_info(const abx_batch *b, abx_batch_info *o) {
+  if (!b || !o) return fail(ABX_ERR_INVALID_ARGUMENT, "batch_get_info: null argument");
+  std::memset(o, 0, sizeof *o);
+  o->n = b->n;
+  for (auto *s : b->sims) {
+    o->cells += s->g->nf;
+    o->state_bytes += (long long)(store_bytes(s->p.storage) * 19 + acc_bytes(s->p.storage) * 4) * s->g->Np;
+  }
+  o->ntiles1 = b->ntiles[0]; o->ntiles2 = b->ntiles[1];
+  o->shape = b->shape; o->grid = b->grid; o->run_ms = b->run_ms; o->kernel_launches = b->launches;
+  return ABX_OK;
+}
+
+// ------------------------------------------------------------------ post-processing
+static PostArgs post_args(const abx_sim &s) {
+  const abx_geom &g = *s.g;
+  PostArgs a{};
+  a.nx = g.nx; a.ny = g.ny; a.nz = g.nz; a.nzp = g.nzp; a.kpad = g.kpad; a.Np = g.Np;
+  a.mask = g.d_mask; a.ns = s.has_ns ? s.d_ns : nullptr; a.opening = g.d_opening;
+  a.acc = s.d_acc; a.acc_double = s.p.storage == ABX_STORE_F64; a.dn = s.nacc > 1 ? s.nacc : 1; a.u0 = s.u0;
+  return a;
+}
+
+static int find_index_ge(const std::vector<float> &a, double v) {  // Array#findIndex(z => z >= v)
+  for (size_t i = 0; i < a.size(); i++) if ((double)a[i] >= v) return (int)i;
+  return -1;
+}
+
+static double js_round(double x) { const double r = std::floor(x); return (x - r >= 0.5) ? r + 1 : r; }
+
+extern "C" int abx_sim_field3d(abx_sim *s, float *spd, float *pst, float *loss, abx_field3d_info *info) {
+  clear_stale_error();
+  if (!s) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_field3d: null simulation");
+  const abx_geom &g = *s->g;
+  CK(cudaSetDevice(g.device), "sim_field3d");
+  const int kB = std::max(2, find_index_ge(g.zc, g.mn[2]) - 2);
+  const int jb = first_ge(g.dc, g.pleat + 2 * g.h);
+  const size_t N = (size_t)g.N;
+  DevBuf scal, out;
+  CK(cudaMalloc(&scal.p, 2 * sizeof(double)), "sim_field3d");
+  float *o[3] = {nullptr, nullptr, nullptr};
+  float *host[3] = {spd, pst, loss};
+  int nout = 0;
+  for (int i = 0; i < 3; i++) nout += host[i] != nullptr;
+  if (nout) {
+    CK(cudaMalloc(&out.p, sizeof(float) * N * nout), "sim_field3d");
+    int k = 0;
+    for (int i = 0; i < 3; i++) if (host[i]) o[i] = (float *)out.p + N * k++;
+  }
+  CK(post_field3d(post_args(*s), kB, jb, (double *)scal.p, o[0], o[1], o[2], s->st), "sim_field3d");
+  s->launches += 2;
+  double sc[2];
+  CK(cudaMemcpyAsync(sc, scal.p, sizeof sc, cudaMemcpyDeviceToHost, s->st), "sim_field3d");
+  for (int i = 0; i < 3; i++)
+    if (host[i]) CK(cudaMemcpyAsync(host[i], o[i], sizeof(float) * N, cudaMemcpyDeviceToHost, s->st), "sim_field3d");
+  CK(cudaStreamSynchronize(s->st), "sim_field3d");
+  s->d2h += (int64_t)(sizeof sc + sizeof(float) * N * nout);
+  if (info) {
+    std::memset(info, 0, sizeof *info);
+    info->nx = g.nx; info->ny = g.ny; info->nz = g.nz; info->kB = kB; info->jm = g.jm; info->top = g.top;
+    info->h = g.h; info->x0 = g.xc[0]; info->d0 = g.dc[0]; info->z0 = g.zc[0]; info->zIn = g.mn[2];
+    info->pleat = g.pleat; info->pin = sc[0]; info->rho_ref = sc[1];
+  }
+  return ABX_OK;
+}
+
+extern "C" int abx_sim_planes(abx_sim *s, float *out, abx_planes_info *info) {
+  clear_stale_error();
+  if (!s) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_planes: null simulation");
+  const abx_geom &g = *s->g;
+  CK(cudaSetDevice(g.device), "sim_planes");
+  double si = 0, sj = 0;
+  int so = 0;
+  for (int i = 0; i < g.nx; i++)
+    for (int j = 0; j < g.ny; j++)
+      if (g.opening[(size_t)i * g.ny + j]) { si += i; sj += j; so++; }
+  const int ic = (int)js_round(si / so), jc = (int)js_round(sj / so);
+  const int jlow = first_ge(g.dc, g.pleat + 12);
+  const size_t n = 6 * (size_t)g.nx * g.nz + 3 * (size_t)g.nz * g.ny;
+  if (out) {
+    DevBuf d;
+    CK(cudaMalloc(&d.p, sizeof(float) * n), "sim_planes");
+    CK(post_planes(post_args(*s), ic, jc, jlow, (float *)d.p, s->st), "sim_planes");
+    s->launches++;
+    CK(cudaMemcpyAsync(out, d.p, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st), "sim_planes");
+    CK(cudaStreamSynchronize(s->st), "sim_planes");
+    s->d2h += (int64_t)(sizeof(float) * n);
+  }
+  if (info) {
+    std::memset(info, 0, sizeof *info);
+    info->ic = ic; info->jc = jc; info->jlow = jlow; info->n1 = g.nx; info->n2 = g.nz;
+    info->lon_n1 = g.nz; info->lon_n2 = g.ny;
+    info->depth_inlet = g.dc[jc]; info->depth_low = g.dc[jlow]; info->x_lon = g.xc[ic];
+  }
+  return ABX_OK;
+}
+
+extern "C" int abx_sim_streamlines(abx_sim *s, int max_seeds, float *pts, float *spd, uint32_t *off, size_t cap_points,
+                                   size_t cap_lines, abx_lines_info *info) {
+  clear_stale_error();
+  if (!s || max_seeds <= 0) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_streamlines: bad argument");
+  const abx_geom &g = *s->g;
+  CK(cudaSetDevice(g.device), "sim_streamlines");
+  // seeds: four per opening cell, kS cells before the box, thinned to about max_seeds (:736-739)
+  const int kS = std::max(2, find_index_ge(g.zc, g.mn[2]) - 3);
+  static const double D[4][2] = {{-0.25, -0.25}, {0.25, -0.25}, {-0.25, 0.25}, {0.25, 0.25}};
+  std::vector<double> all;
+  for (int i = 0; i < g.nx; i++)
+    for (int j = 0; j < g.ny; j++)
+      if (g.opening[(size_t)i * g.ny + j])
+        for (int d = 0; d < 4; d++) { all.push_back(i + D[d][0]); all.push_back(j + D[d][1]); all.push_back(kS); }
+  const int nall = (int)(all.size() / 3);
+  const double stride = std::max(1.0, (double)nall / max_seeds);
+  std::vector<double> sel;
+  for (double x = 0; x < nall; x += stride) {
+    const size_t k = (size_t)std::floor(x);
+    sel.insert(sel.end(), all.begin() + 3 * k, all.begin() + 3 * k + 3);
+  }
+  const int nsel = (int)(sel.size() / 3);
+  std::vector<int> cnt(std::max(nsel, 1));
+  std::vector<double> P((size_t)std::max(nsel, 1) * 4 * kMaxLinePoints);
+  if (nsel) {
+    DevBuf dseeds, dpts, dcnt;
+    CK(cudaMalloc(&dseeds.p, sizeof(double) * sel.size()), "sim_streamlines");
+    CK(cudaMalloc(&dpts.p, sizeof(double) * P.size()), "sim_streamlines");
+    CK(cudaMalloc(&dcnt.p, sizeof(int) * nsel), "sim_streamlines");
+    CK(cudaMemcpyAsync(dseeds.p, sel.data(), sizeof(double) * sel.size(), cudaMemcpyHostToDevice, s->st), "sim_streamlines");
+    CK(post_streamlines(post_args(*s), (const double *)dseeds.p, nsel, g.top, (double *)dpts.p, (int *)dcnt.p, s->st),
+       "sim_streamlines");
+    s->launches++;
+    CK(cudaMemcpyAsync(cnt.data(), dcnt.p, sizeof(int) * nsel, cudaMemcpyDeviceToHost, s->st), "sim_streamlines");
+    CK(cudaMemcpyAsync(P.data(), dpts.p, sizeof(double) * P.size(), cudaMemcpyDeviceToHost, s->st), "sim_streamlines");
+    CK(cudaStreamSynchronize(s->st), "sim_streamlines");
+    s->h2d += (int64_t)(sizeof(double) * sel.size());
+    s->d2h += (int64_t)(sizeof(int) * nsel + sizeof(double) * P.size());
+  }
+  // lines of at least two points, in model coordinates (:752-756)
+  size_t np = 0, nl = 0;
+  bool fits = true;
+  if (off && cap_lines >= 1) off[0] = 0; else fits = false;
+  for (int sd = 0; sd < nsel; sd++) {
+    const int m = cnt[sd];
+    if (m < 2) continue;
+    const double *Q = P.data() + (size_t)sd * 4 * kMaxLinePoints;
+    for (int q = 0; q < m; q++) {
+      if (np + q < cap_points && pts && spd) {
+        double mm[3];
+        g.fr.model((double)g.xc[0] + Q[4 * q] * g.h, (double)g.dc[0] + Q[4 * q + 1] * g.h,
+                   (double)g.zc[0] + Q[4 * q + 2] * g.h, mm);
+        pts[3 * (np + q)] = (float)mm[0]; pts[3 * (np + q) + 1] = (float)mm[1]; pts[3 * (np + q) + 2] = (float)mm[2];
+        spd[np + q] = (float)Q[4 * q + 3];
+      } else {
+        fits = false;
+      }
+    }
+    np += m;
+    nl++;
+    if (off && nl < cap_lines) off[nl] = (uint32_t)np; else fits = false;
+  }
+  if (info) { info->seeds_opening = nall; info->seeds_traced = nsel; info->n_lines = (int)nl; info->n_points = (int)np; }
+  if (!fits)
+    return fail(ABX_ERR_INVALID_ARGUMENT, "sim_streamlines: %zu points / %zu lines need larger buffers", np, nl + 1);
   return ABX_OK;
 }

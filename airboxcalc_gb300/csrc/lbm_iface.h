@@ -84,6 +84,16 @@ cudaError_t launch_evaluate(int storage, const StateArgs &a, const EvalArgs &e, 
 cudaError_t launch_step_fast(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, const TmaBlob *tma,
                              cudaStream_t st);
 
+// One step of many domains in one launch (lbm_fast.cu; float32, float16, bfloat16 storage).
+// vars: device array of the domains' StepArgs; tiles[t] = {domain, first segment} of 8*spw segments;
+// grid blocks loop over the tiles (grid >= ntiles: one tile per block).  shape (0..kBatchShapes-1)
+// selects segments per warp (spw) and the resident blocks per SM the kernel's registers are sized for.
+constexpr int kBatchShapes = 3;
+int batch_shape_spw(int shape);
+int batch_shape_minblocks(int shape);
+cudaError_t launch_step_batch(int storage, bool odd, bool acc, int shape, const StepArgs *vars, const uint2 *tiles,
+                              uint32_t ntiles, uint32_t grid, cudaStream_t st);
+
 // Mask construction (lbm_exact.cu): class bytes (0 not fluid, 1 bulk, 2 inlet,
 // 3 outlet, 4 filter; index (i*ny+j)*nz+k) -> padded mask words, cell (i,j,k)
 // at padded index (i*ny+j)*nzp + k + kpad.
@@ -117,6 +127,29 @@ cudaError_t run_voxelizer(const VoxJob &job, VoxOut &out, cudaStream_t st);
 // Returns an abx_status value; msg receives the text of a failure.
 int voxelize_static(const float *d_tris, size_t nfloats, const double origin[3], double h, int nx, int ny, int nz,
                     uint8_t *d_vox, cudaStream_t st, char *msg, size_t msg_len);
+
+// ---------------------------------------------------------------- post-processing (postproc.cu)
+struct PostArgs {
+  int nx, ny, nz;
+  int64_t nzp, kpad, Np;
+  const uint32_t *mask;      // padded; nonzero: fluid
+  const float *ns;           // padded partial bounce-back, or null (cells with ns > 0.5 count as no air)
+  const uint8_t *opening;    // nx*ny
+  const void *acc;           // running sums [4][Np]
+  int acc_double;            // sums in float64 (the float64 run)
+  double dn;                 // averaged steps (>= 1)
+  double u0;
+};
+constexpr int kMaxLinePoints = 2001;   // points one streamline can keep (6000 steps, every 3rd, plus the last)
+// field3d: d_scal receives pin and rhoRef; spd/pst/loss (nx*ny*nz floats, may be null)
+cudaError_t post_field3d(const PostArgs &a, int kB, int jb, double *d_scal, float *spd, float *pst, float *loss,
+                         cudaStream_t st);
+// cut planes: out = planInlet (speed, ua, ub; nx*nz each), planLow (same), lon (speed, ua, ub; nz*ny each)
+cudaError_t post_planes(const PostArgs &a, int ic, int jc, int jlow, float *out, cudaStream_t st);
+// streamlines: seeds (3 doubles each, grid-cell coordinates) -> pts (4 doubles per point, kMaxLinePoints
+// per seed) and count (points per seed)
+cudaError_t post_streamlines(const PostArgs &a, const double *seeds, int nseeds, int top, double *pts, int *count,
+                             cudaStream_t st);
 
 // ---------------------------------------------------------------- warm start
 // The padded grid as the resampling kernels see it (warmstart.cu).

@@ -50,18 +50,16 @@ template <class L> __device__ __forceinline__ CollideParams<L> make_params(const
 #endif
 constexpr int kStepSpw = ABX_STEP_SPW;
 
-template <int K, bool ODD, bool ACC, bool HAS_NS>
-__global__ void __launch_bounds__(256, ABX_STEP_MINBLOCKS) aa_step_kernel(const StepArgs a) {
+// One warp's share of a step: SPW segments starting at s0 of the domain described by `a`.
+template <int K, bool ODD, bool ACC, bool HAS_NS, int SPW, class Args>
+__device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, const uint32_t lane) {
   using S = Store<K>;
   using T = typename S::T;
   using L = typename S::L;
   using Acc = typename S::Acc;
-  constexpr int SPW = kStepSpw;
-  const uint32_t s0 = (blockIdx.x * 8u + (threadIdx.x >> 5)) * SPW;
   if (s0 >= a.nseg) return;
   // the run-state word changes only between launches: a plain load issued together with the segment's
   const int halted = a.status ? *a.status : 0;
-  const uint32_t lane = threadIdx.x & 31;
   uint2 sg[SPW];
 #pragma unroll
   for (int j = 0; j < SPW; j++) sg[j] = (s0 + j < a.nseg) ? a.seg[s0 + j] : make_uint2(0, 0);
@@ -126,6 +124,31 @@ __global__ void __launch_bounds__(256, ABX_STEP_MINBLOCKS) aa_step_kernel(const 
       acc[2u * Np + p[j]] = (Acc)((L)av[j][2] + uz);
       acc[3u * Np + p[j]] = (Acc)((L)av[j][3] + rho);
     }
+  }
+}
+
+template <int K, bool ODD, bool ACC, bool HAS_NS>
+__global__ void __launch_bounds__(256, ABX_STEP_MINBLOCKS) aa_step_kernel(const StepArgs a) {
+  step_warp<K, ODD, ACC, HAS_NS, kStepSpw>(a, (blockIdx.x * 8u + (threadIdx.x >> 5)) * kStepSpw, threadIdx.x & 31);
+}
+
+// One step of many domains in one launch.  tiles[t] = {variant, first segment}: a block takes 8*SPW
+// consecutive segments of one variant; with fewer blocks than tiles the blocks loop over the tile list
+// (persistent).  The variant's arguments are staged in shared memory for the block.  SPW (segments
+// per warp) and MINB (resident blocks per SM the registers are sized for) are the autotuner's knobs.
+template <int K, bool ODD, bool ACC, int SPW, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+    aa_step_batch_kernel(const StepArgs *__restrict__ vars, const uint2 *__restrict__ tiles, uint32_t ntiles) {
+  __shared__ __align__(16) StepArgs sa;
+  static_assert(sizeof(StepArgs) % 8 == 0 && sizeof(StepArgs) / 8 <= 256, "StepArgs staging");
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint2 tile = tiles[t];
+    __syncthreads();
+    if (threadIdx.x < sizeof(StepArgs) / 8)
+      reinterpret_cast<unsigned long long *>(&sa)[threadIdx.x] =
+          reinterpret_cast<const unsigned long long *>(vars + tile.x)[threadIdx.x];
+    __syncthreads();
+    step_warp<K, ODD, ACC, false, SPW>(sa, tile.y + (threadIdx.x >> 5) * SPW, threadIdx.x & 31);
   }
 }
 

@@ -11,7 +11,7 @@
 //   head     conv(c0 -> 4), no activation
 // Every conv is 3x3x3 with padding 1 and a ReLU except the head.
 // Input channels: fluid, inlet, outlet, filter fraction, wall distance, K,
-// grid extent (3); output: u / u0 (3) and (rho - 1) / (15 u0^2).
+// grid extent (3); output: u / u0 (3) and (rho - 1) / (5 u0^2).
 #pragma once
 #include <cuda_runtime_api.h>
 #include <stdint.h>

@@ -1,0 +1,235 @@
+// postproc.cu - post-processing of the time-averaged fields on the device
+// (compiled with -fmad=false: float64 arithmetic in the reference's order).
+//
+//   field3d      src/engine.js:698-719: |u|/u0, static pressure and total-pressure
+//                loss on the whole grid (NaN where there is no air)
+//   planes       src/engine.js:662-680: the cut planes planInlet, planLow, lon
+//   streamlines  src/engine.js:721-758: RK2 traces of the averaged velocity from
+//                the inlet opening, one thread per seed
+//
+// The averages are read as the reference holds them: the Float32Array of
+// simulate() (sum / nacc rounded to float32, :356).  Sums the reference takes
+// in one loop (the inlet's mass-weighted total pressure, the reference
+// density under the filter) run in one thread, in its order.  Math.hypot
+// follows V8's published algorithm (scale by the largest magnitude,
+// Kahan-compensated sum of squares).
+#include <math.h>
+#include <stdint.h>
+
+#include "lbm_iface.h"
+
+namespace abx {
+
+template <typename Acc>
+struct AvgView {
+  const Acc *acc;
+  int64_t Np;
+  double dn;
+  __device__ __forceinline__ double operator()(int comp, int64_t p) const {
+    return (double)(float)((double)acc[comp * Np + p] / dn);
+  }
+};
+
+__device__ __forceinline__ double js_hypot3(double x, double y, double z) {
+  const double a[3] = {fabs(x), fabs(y), fabs(z)};
+  double mx = 0;
+  for (int i = 0; i < 3; i++) {
+    if (isnan(a[i])) return NAN;
+    if (a[i] > mx) mx = a[i];
+  }
+  if (isinf(mx)) return INFINITY;
+  if (mx == 0) return 0;
+  double sum = 0, comp = 0;
+  for (int i = 0; i < 3; i++) {
+    const double n = a[i] / mx;
+    const double summand = n * n - comp;
+    const double pre = sum + summand;
+    comp = (pre - sum) - summand;
+    sum = pre;
+  }
+  return sqrt(sum) * mx;
+}
+
+__device__ __forceinline__ double js_round(double x) {
+  const double r = floor(x);
+  return (x - r >= 0.5) ? r + 1 : r;
+}
+
+__device__ __forceinline__ bool air(const PostArgs &a, int64_t p) {
+  return a.mask[p] != 0u && !(a.ns && a.ns[p] > 0.5f);
+}
+__device__ __forceinline__ int64_t padded(const PostArgs &a, int i, int j, int k) {
+  return ((int64_t)i * a.ny + j) * a.nzp + k + a.kpad;
+}
+
+// out[0] = pin (mass-flow-weighted total pressure at k = kB over the opening, :705-711),
+// out[1] = rhoRef (mean density on layer jb, :658-659)
+template <typename Acc>
+__global__ void post_scalars_kernel(const PostArgs a, int kB, int jb, double *out) {
+  const AvgView<Acc> U{(const Acc *)a.acc, a.Np, a.dn};
+  double pb = 0;
+  int pbN = 0;
+  for (int i = 0; i < a.nx; i++)
+    for (int k = 0; k < a.nz; k++) {
+      const int64_t p = padded(a, i, jb, k);
+      if (air(a, p)) { pb += U(3, p); pbN++; }
+    }
+  double pin = 0, win = 0;
+  for (int i = 0; i < a.nx; i++)
+    for (int j = 0; j < a.ny; j++) {
+      if (!a.opening[(int64_t)i * a.ny + j]) continue;
+      const int64_t p = padded(a, i, j, kB);
+      if (!air(a, p)) continue;
+      const double ux = U(0, p), uy = U(1, p), uz = U(2, p);
+      const double w = uz > 0 ? uz : 0;
+      pin += w * (U(3, p) / 3 + 0.5 * (ux * ux + uy * uy + uz * uz));
+      win += w;
+    }
+  out[0] = pin / (win > 1e-12 ? win : 1e-12);
+  out[1] = pb / pbN;
+}
+
+template <typename Acc>
+__global__ void field3d_kernel(const PostArgs a, int kB, const double *scal, float *spd, float *pst, float *loss) {
+  const AvgView<Acc> U{(const Acc *)a.acc, a.Np, a.dn};
+  const int64_t N = (int64_t)a.nx * a.ny * a.nz;
+  const double q = 0.5 * a.u0 * a.u0, pin = scal[0], rhoRef = scal[1];
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(c % a.nz);
+    const int64_t ij = c / a.nz;
+    const int64_t p = ij * a.nzp + k + a.kpad;
+    float s = NAN, ps = NAN, l = NAN;
+    if (air(a, p) && k >= kB) {
+      const double ux = U(0, p), uy = U(1, p), uz = U(2, p), rho = U(3, p);
+      s = (float)(js_hypot3(ux, uy, uz) / a.u0);
+      ps = (float)((rho - rhoRef) / 3 / q);
+      l = (float)((pin - (rho / 3 + 0.5 * (ux * ux + uy * uy + uz * uz))) / q);
+    }
+    if (spd) spd[c] = s;
+    if (pst) pst[c] = ps;
+    if (loss) loss[c] = l;
+  }
+}
+
+// planInlet (j = jc), planLow (j = jlow): speed, ua = ux/u0, ub = uz/u0 over (i, k);
+// lon (i = ic): speed, ua = uz/u0, ub = uy/u0 over (k, j).
+template <typename Acc>
+__global__ void planes_kernel(const PostArgs a, int ic, int jc, int jlow, float *out) {
+  const AvgView<Acc> U{(const Acc *)a.acc, a.Np, a.dn};
+  const int64_t P = (int64_t)a.nx * a.nz, Q = (int64_t)a.nz * a.ny, n = 2 * P + Q;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    float *s, *ua, *ub;
+    int64_t p;
+    bool lon = t >= 2 * P;
+    if (!lon) {
+      const int pl = (int)(t / P);
+      const int64_t x = t % P;
+      s = out + pl * 3 * P + x; ua = s + P; ub = ua + P;
+      p = padded(a, (int)(x / a.nz), pl == 0 ? jc : jlow, (int)(x % a.nz));
+    } else {
+      const int64_t x = t - 2 * P;
+      s = out + 6 * P + x; ua = s + Q; ub = ua + Q;
+      p = padded(a, ic, (int)(x % a.ny), (int)(x / a.ny));
+    }
+    if (!air(a, p)) { *s = NAN; *ua = 0.0f; *ub = 0.0f; continue; }
+    const double ux = U(0, p) / a.u0, uy = U(1, p) / a.u0, uz = U(2, p) / a.u0;
+    *s = (float)js_hypot3(ux, uy, uz);
+    *ua = (float)(lon ? uz : ux);
+    *ub = (float)(lon ? uy : uz);
+  }
+}
+
+template <typename Acc>
+__device__ double trace_vel(const PostArgs &a, const AvgView<Acc> &U, double x, double y, double z, double out[3]) {
+  const double fi0 = floor(x), fj0 = floor(y), fk0 = floor(z);
+  const double fx = x - fi0, fy = y - fj0, fz = z - fk0;
+  const int i0 = (int)fi0, j0 = (int)fj0, k0 = (int)fk0;
+  out[0] = out[1] = out[2] = 0;
+  double wsum = 0;
+  for (int da = 0; da < 2; da++)
+    for (int db = 0; db < 2; db++)
+      for (int dc = 0; dc < 2; dc++) {
+        const int i = i0 + da, j = j0 + db, k = k0 + dc;
+        if (i < 0 || j < 0 || k < 0 || i >= a.nx || j >= a.ny || k >= a.nz) continue;
+        const double w = (da ? fx : 1 - fx) * (db ? fy : 1 - fy) * (dc ? fz : 1 - fz);
+        const int64_t p = padded(a, i, j, k);
+        if (!air(a, p)) continue;
+        out[0] += w * U(0, p);
+        out[1] += w * U(1, p);
+        out[2] += w * U(2, p);
+        wsum += w;
+      }
+  return wsum;
+}
+
+__device__ __forceinline__ bool trace_inside(const PostArgs &a, double x, double y, double z) {
+  const double ri = js_round(x), rj = js_round(y), rk = js_round(z);
+  if (ri < 0 || rj < 0 || rk < 0 || ri >= a.nx || rj >= a.ny || rk >= a.nz) return false;
+  return air(a, padded(a, (int)ri, (int)rj, (int)rk));
+}
+
+// One thread per seed: the trace of :739-751, up to kMaxLinePoints points (x, y, z, |u|/u0) in
+// grid-cell coordinates into the seed's slot; count[s] = points kept.
+template <typename Acc>
+__global__ void streamline_kernel(const PostArgs a, const double *seeds, int nseeds, int top, double *pts,
+                                  int *count) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseeds) return;
+  const AvgView<Acc> U{(const Acc *)a.acc, a.Np, a.dn};
+  double x = seeds[3 * s], y = seeds[3 * s + 1], z = seeds[3 * s + 2], v1[3], v2[3];
+  double *P = pts + (int64_t)s * 4 * kMaxLinePoints;
+  const double ds = 0.35;
+  int m = 0;
+  for (int st = 0; st < 6000; st++) {
+    if (!trace_inside(a, x, y, z) || trace_vel(a, U, x, y, z, v1) < 0.3) break;
+    const double m1 = js_hypot3(v1[0], v1[1], v1[2]);
+    if (m1 < 0.01 * a.u0) break;
+    if (st % 3 == 0) { P[4 * m] = x; P[4 * m + 1] = y; P[4 * m + 2] = z; P[4 * m + 3] = m1 / a.u0; m++; }
+    const double xm = x + 0.5 * ds * v1[0] / m1, ym = y + 0.5 * ds * v1[1] / m1, zm = z + 0.5 * ds * v1[2] / m1;
+    if (trace_vel(a, U, xm, ym, zm, v2) < 0.3) break;
+    const double m2 = js_hypot3(v2[0], v2[1], v2[2]);
+    if (m2 < 0.01 * a.u0) break;
+    x += ds * v2[0] / m2;
+    y += ds * v2[1] / m2;
+    z += ds * v2[2] / m2;
+    if (y < top + 0.5) { P[4 * m] = x; P[4 * m + 1] = y; P[4 * m + 2] = z; P[4 * m + 3] = m2 / a.u0; m++; break; }
+  }
+  count[s] = m;
+}
+
+static unsigned grid_of(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b > 152 * 8) b = 152 * 8;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+cudaError_t post_field3d(const PostArgs &a, int kB, int jb, double *d_scal, float *spd, float *pst, float *loss,
+                         cudaStream_t st) {
+  const int64_t N = (int64_t)a.nx * a.ny * a.nz;
+  if (a.acc_double) {
+    post_scalars_kernel<double><<<1, 1, 0, st>>>(a, kB, jb, d_scal);
+    field3d_kernel<double><<<grid_of(N), 256, 0, st>>>(a, kB, d_scal, spd, pst, loss);
+  } else {
+    post_scalars_kernel<float><<<1, 1, 0, st>>>(a, kB, jb, d_scal);
+    field3d_kernel<float><<<grid_of(N), 256, 0, st>>>(a, kB, d_scal, spd, pst, loss);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t post_planes(const PostArgs &a, int ic, int jc, int jlow, float *out, cudaStream_t st) {
+  const int64_t n = 2 * (int64_t)a.nx * a.nz + (int64_t)a.nz * a.ny;
+  if (a.acc_double) planes_kernel<double><<<grid_of(n), 256, 0, st>>>(a, ic, jc, jlow, out);
+  else planes_kernel<float><<<grid_of(n), 256, 0, st>>>(a, ic, jc, jlow, out);
+  return cudaGetLastError();
+}
+
+cudaError_t post_streamlines(const PostArgs &a, const double *seeds, int nseeds, int top, double *pts, int *count,
+                             cudaStream_t st) {
+  if (nseeds <= 0) return cudaSuccess;
+  const unsigned blocks = (unsigned)((nseeds + 31) / 32);
+  if (a.acc_double) streamline_kernel<double><<<blocks, 32, 0, st>>>(a, seeds, nseeds, top, pts, count);
+  else streamline_kernel<float><<<blocks, 32, 0, st>>>(a, seeds, nseeds, top, pts, count);
+  return cudaGetLastError();
+}
+
+}  // namespace abx

@@ -6,7 +6,7 @@
 //                solid voxel (jump flooding, in grid cells), the filter's K
 //                and the grid's extent
 //   ws_targets   training target per voxel: the time-averaged u / u0 and
-//                (rho - 1) / (15 u0^2) over the footprint's fluid cells, and
+//                (rho - 1) / (5 u0^2) over the footprint's fluid cells, and
 //                the fluid fraction as the loss weight
 //   ws_apply     warm start: the predicted field, trilinearly interpolated
 //                to every fluid cell (weighted by voxel fluid fraction), as
@@ -118,7 +118,7 @@ template <typename Acc>
 __global__ void targets_kernel(const GridDesc g, const Acc *__restrict__ acc, double inv_n, double u0, int R,
                                float *__restrict__ t, float *__restrict__ m) {
   const int V = R * R * R;
-  const double su = 1.0 / u0, sr = 1.0 / (15.0 * u0 * u0);
+  const double su = 1.0 / u0, sr = 1.0 / (5.0 * u0 * u0);
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
     const int c = v % R, b = (v / R) % R, a = v / (R * R);
     int i0, i1, j0, j1, k0, k1;
@@ -186,7 +186,7 @@ __global__ void apply_kernel(const StateArgs a, const GridDesc g, const float *_
       for (int q = 0; q < 4; q++) p[q] = pred[q * V + v];
     }
     L ux = (L)(p[0] * u0), uy = (L)(p[1] * u0), uz = (L)(p[2] * u0);
-    L rho = (L)(1.0 + 15.0 * u0 * u0 * p[3]);
+    L rho = (L)(1.0 + 5.0 * u0 * u0 * p[3]);
     // keep the start inside the lattice's stable range
     const L sp = sqrt(ux * ux + uy * uy + uz * uz), cap = (L)0.2;
     if (!(sp <= cap)) {

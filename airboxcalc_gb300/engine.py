@@ -269,6 +269,46 @@ class Simulation:
                           "yaw": fr.yaw},
                 "_detail": {k: getattr(m, k) for k in ("wm", "cm", "n", "cn", "pinN", "pbN", "jb")}}
 
+    def field3d(self) -> dict:
+        """field3d (src/engine.js:698-719): spd, pst, loss on the whole grid (NaN = no air)."""
+        g = self.g
+        out = [np.empty(g.N, np.float32) for _ in range(3)]
+        i = A.Field3DInfo()
+        _check(A.load().abx_sim_field3d(self._h, *(_ptr(o) for o in out), C.byref(i)))
+        return {"nx": g.nx, "ny": g.ny, "nz": g.nz, "h": i.h, "x0": i.x0, "d0": i.d0, "z0": i.z0,
+                "spd": out[0], "pst": out[1], "loss": out[2], "jm": i.jm, "top": i.top, "pleat": i.pleat,
+                "kB": i.kB, "zIn": i.zIn, "_pin": i.pin, "_rhoRef": i.rho_ref}
+
+    def planes(self) -> dict:
+        """The cut planes of evaluate (src/engine.js:662-680): planInlet, planLow, lon."""
+        g = self.g
+        P, Q = g.nx * g.nz, g.nz * g.ny
+        buf = np.empty(6 * P + 3 * Q, np.float32)
+        i = A.PlanesInfo()
+        _check(A.load().abx_sim_planes(self._h, _ptr(buf), C.byref(i)))
+
+        def plan(o, depth):
+            return {"speed": buf[o:o + P], "ua": buf[o + P:o + 2 * P], "ub": buf[o + 2 * P:o + 3 * P],
+                    "n1": g.nx, "n2": g.nz, "depth": depth}
+        lon = {"speed": buf[6 * P:6 * P + Q], "ua": buf[6 * P + Q:6 * P + 2 * Q], "ub": buf[6 * P + 2 * Q:],
+               "n1": g.nz, "n2": g.ny, "x": i.x_lon}
+        return {"planInlet": plan(0, i.depth_inlet), "planLow": plan(3 * P, i.depth_low), "lon": lon,
+                "_ic": i.ic, "_jc": i.jc, "_jlow": i.jlow}
+
+    def streamlines(self, maxSeeds: int = 220) -> dict:
+        """streamlines (src/engine.js:721-758), traced on the GPU: pts (model coordinates), spd, off."""
+        i = A.LinesInfo()
+        L = A.load()
+        rc = L.abx_sim_streamlines(self._h, maxSeeds, None, None, None, 0, 0, C.byref(i))
+        if rc not in (A.OK, A.ERR_INVALID_ARGUMENT):
+            _check(rc)
+        pts = np.empty(3 * max(i.n_points, 1), np.float32)
+        spd = np.empty(max(i.n_points, 1), np.float32)
+        off = np.empty(i.n_lines + 1, np.uint32)
+        _check(L.abx_sim_streamlines(self._h, maxSeeds, _ptr(pts), _ptr(spd), _ptr(off), i.n_points,
+                                     i.n_lines + 1, C.byref(i)))
+        return {"pts": pts[:3 * i.n_points], "spd": spd[:i.n_points], "off": off}
+
     def set_timing(self, on: bool = True):
         _check(A.load().abx_sim_set_timing(self._h, 1 if on else 0))
 
@@ -296,17 +336,24 @@ def cpuStep(S: Simulation, n: int = 1, accumulate: bool = False):
     S.step(n, accumulate)
 
 
-def simulate(g: Geometry, p: dict, onProgress: Optional[Callable] = None, ns=None) -> dict:
-    """simulate(g, p, onProgress, ns) (src/engine.js:341-358): the step loop and evaluate()."""
+def simulate(g: Geometry, p: dict, onProgress: Optional[Callable] = None, ns=None, full: bool = True) -> dict:
+    """simulate(g, p, onProgress, ns) (src/engine.js:341-358): the step loop and evaluate().
+    With full=False only the KPIs, filter map and history are read back (no planes, field3d, lines)."""
     if g is None:
         raise AirboxError(A.ERR_NOT_PREPARED, "Bitte zuerst die Geometrie prüfen.")
     S = Simulation(g, p, ns)
     S.run(onProgress)
-    res = S.evaluate()
+    res = evaluate(S) if full else S.evaluate()
     res["device"] = "GPU"
     return res
 
 
 def evaluate(S: Simulation) -> dict:
-    """evaluate() (src/engine.js:632-691) of a finished simulation: KPIs and the filter map."""
-    return S.evaluate()
+    """evaluate() (src/engine.js:632-691) of a finished simulation: KPIs, filter map, history, the cut
+    planes (planInlet, planLow, lon), the 3-D fields (vol, field3d :698-719) and the streamlines (lines)."""
+    res = S.evaluate()
+    pl = S.planes()
+    res.update({k: pl[k] for k in ("planInlet", "planLow", "lon")})
+    res["vol"] = S.field3d()
+    res["lines"] = S.streamlines()
+    return res

@@ -6,9 +6,9 @@ The reference has no counterpart: engine.js starts every run from f = w_i
 (src/engine.js:261) and runs the fixed steps/avg schedule (:341-358).  Here a
 3-D convolutional encoder-decoder predicts the time-averaged velocity and
 density from the voxelized geometry; the solve starts from their equilibrium,
-runs averaging windows until two consecutive windows agree on gamma core and
-zeta, and falls back to the uniform start and the full schedule when they do
-not.  Training, inference and the initialisation run in the library's CUDA
+settles, then grows a running average until its gamma core and zeta stop
+moving, and falls back to the uniform start and the full schedule when they
+do not.  Training, inference and the initialisation run in the library's CUDA
 kernels; this module only moves parameters and drives the loop.
 
 Command line (trains on the GPU and writes the weights):
@@ -35,8 +35,8 @@ WEIGHTS = os.path.join(HERE, "weights", "warmstart_r64_b16_l4.npz")
 # The reference's run parameters (the fixed schedule the plain solve follows).
 RUN = dict(K=3, aniso=10, u=0.06, tau=0.51, steps=6000, avg=2000, every=150)
 K_CHOICES = (1.5, 3.0, 6.0)
-# Stop rule of the windowed run.
-CONVERGE = dict(window=250, min_windows=2, max_steps=3000, tol=0.005)
+# Stop rule of the convergence run: settle, then a running average checked every window.
+CONVERGE = dict(settle=1000, window=500, min_avg=1000, max_steps=4000, tol=0.01)
 
 
 def variant(seed: int, dx: float = 2.0):
@@ -148,7 +148,7 @@ def _metrics(m: A.Metrics) -> dict:
 
 def _converge_params(**kw) -> A.ConvergeParams:
     c = dict(CONVERGE, **kw)
-    return A.ConvergeParams(window=int(c["window"]), min_windows=int(c["min_windows"]),
+    return A.ConvergeParams(settle=int(c["settle"]), window=int(c["window"]), min_avg=int(c["min_avg"]),
                             max_steps=int(c["max_steps"]), tol=float(c["tol"]))
 
 
@@ -158,7 +158,7 @@ def warm_start(sim: E.Simulation, net: Net):
 
 
 def converge(sim: E.Simulation, **kw) -> dict:
-    """Averaging windows from the current state until two consecutive windows agree (abx_sim_converge)."""
+    """Settle, then a running average until its KPIs stop moving (abx_sim_converge)."""
     r = A.ConvergeResult()
     E._check(A.load().abx_sim_converge(sim._h, C.byref(_converge_params(**kw)), C.byref(r)))
     return {"metrics": _metrics(r.metrics), "steps": r.steps, "windows": r.windows, "converged": bool(r.converged),

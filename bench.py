@@ -261,6 +261,183 @@ def study_converge(spec, run, desc, storages=("f32", "f16", "bf16"), ladder=(600
     return out
 
 
+# Stop rules compared by the warm-start study; the first is the library's default.
+WARM_RULES = (dict(settle=1000, window=500, min_avg=1000, max_steps=4000, tol=0.01),
+              dict(settle=1000, window=500, min_avg=1500, max_steps=4500, tol=0.005),
+              dict(settle=500, window=500, min_avg=1000, max_steps=4000, tol=0.01))
+
+
+def _rel_err(m, ref):
+    return (abs(m["gammaCore"] - ref["gammaCore"]) / abs(ref["gammaCore"]),
+            abs(m["zeta"] - ref["zeta"]) / abs(ref["zeta"]))
+
+
+def study_warmstart(seeds, weights: str, rules=WARM_RULES, uniform: bool = True, noise: bool = True,
+                    quiet: bool = False):
+    """Time to converged gamma core / zeta: float16 storage + learned warm start + convergence run
+    (abx_sim_solve_warm) against the plain float32 run on the reference's fixed schedule, on held-out
+    seeded airboxes at dx 2 mm.  Wall times are host clocks around the solve (prepare excluded), each
+    taken after one untimed solve of the same arm on the same simulation object (CUDA graphs built).
+    With `uniform`, the same convergence run from f = w_i (float16) shows what the network adds.  With
+    `noise`, the plain float32 run continued to 8000 steps (averaging 6000-8000) measures how far the
+    reference's own KPIs move between consecutive 2000-step windows: the noise floor of the +-1 % test."""
+    from airboxcalc_gb300 import airboxgen as ag
+    from airboxcalc_gb300 import engine as E
+    from airboxcalc_gb300 import warmstart as W
+    net = W.Net.load(weights)
+    rows = []
+    for seed in seeds:
+        spec, K = W.variant(seed, 2.0)
+        run = dict(W.RUN, K=K)
+        try:
+            g = E.prepare({"tris": ag.build_airbox(spec), **spec.prepare_params(), "maxCells": 1e10})
+            P = E.Simulation(g, run)
+            P.run()
+            P.reset()
+            t0 = time.perf_counter()
+            P.run()
+            ref = P.evaluate()["metrics"]
+            plain_ms = (time.perf_counter() - t0) * 1e3
+        except E.AirboxError as e:
+            rows.append({"seed": seed, "skipped": e.code})
+            continue
+        row = {"seed": seed, "K": K, "NF": P.NF, "plain_f32_ms": round(plain_ms, 2),
+               "ref": {"gammaCore": ref["gammaCore"], "zeta": ref["zeta"]}}
+        if noise:
+            P.clear_acc()
+            P.step(2000, True)
+            eg, ez = _rel_err(P.evaluate()["metrics"], ref)
+            row["noise_f32"] = {"ms": plain_ms, "steps": 8000, "err_gammaCore": float(f"{eg:.3e}"),
+                                "err_zeta": float(f"{ez:.3e}")}
+        del P
+        S = E.Simulation(g, dict(run, storage="f16"))
+        for i, rule in enumerate(rules):
+            W.solve_warm(S, net, **rule)
+            r = W.solve_warm(S, net, **rule)
+            eg, ez = _rel_err(r["metrics"], ref)
+            row[f"warm{i}"] = {"ms": round(r["total_ms"], 2), "steps": r["steps"], "fell_back": r["fell_back"],
+                               "infer_ms": round(r["infer_ms"], 3), "err_gammaCore": float(f"{eg:.3e}"),
+                               "err_zeta": float(f"{ez:.3e}")}
+        if uniform:
+            rule = rules[0]
+            S.reset()
+            W.converge(S, **rule)
+            S.reset()
+            t0 = time.perf_counter()
+            r = W.converge(S, **rule)
+            ms = (time.perf_counter() - t0) * 1e3
+            eg, ez = _rel_err(r["metrics"], ref)
+            row["uniform0"] = {"ms": round(ms, 2), "steps": r["steps"], "converged": r["converged"],
+                               "err_gammaCore": float(f"{eg:.3e}"), "err_zeta": float(f"{ez:.3e}")}
+        rows.append(row)
+        if not quiet:
+            print(json.dumps(row), flush=True)
+    done = [r for r in rows if "skipped" not in r]
+
+    def summary(key):
+        xs = [r[key] for r in done if key in r]
+        if not xs:
+            return None
+        ok = [max(x["err_gammaCore"], x["err_zeta"]) < 0.01 for x in xs]
+        sp = [r["plain_f32_ms"] / r[key]["ms"] for r in done if key in r]
+        out = {"n": len(xs), "within_1pct": round(sum(ok) / len(xs), 3),
+               "median_speedup_vs_plain_f32": round(statistics.median(sp), 2),
+               "mean_wall_speedup": round(sum(r["plain_f32_ms"] for r in done) / sum(x["ms"] for x in xs), 2),
+               "median_err_gammaCore": float(f"{statistics.median(x['err_gammaCore'] for x in xs):.3e}"),
+               "median_err_zeta": float(f"{statistics.median(x['err_zeta'] for x in xs):.3e}"),
+               "median_steps": statistics.median(x["steps"] for x in xs)}
+        if "fell_back" in xs[0]:
+            out["fallback_rate"] = round(sum(x["fell_back"] for x in xs) / len(xs), 3)
+        return out
+
+    summ = {"study": "warmstart", "seeds": f"{min(seeds)}..{max(seeds)}", "evaluated": len(done),
+            "skipped_unstable_or_leaking": len(rows) - len(done), "weights": os.path.relpath(weights, ROOT),
+            "rules": [dict(r) for r in rules]}
+    for i in range(len(rules)):
+        summ[f"warm{i}_f16"] = summary(f"warm{i}")
+    if uniform:
+        summ["uniform0_f16"] = summary("uniform0")
+    if noise:
+        summ["noise_floor_f32_next_window"] = summary("noise_f32")
+    print(json.dumps(summ), flush=True)
+    return summ, rows
+
+
+def batch_variants(n: int, seed0: int = 7000):
+    """The variant table of the batched run: seeded airboxes with dx in [2, 4) mm and K in {1.5, 3, 6}."""
+    from airboxcalc_gb300 import airboxgen as ag
+    out = []
+    for v in range(n):
+        seed = seed0 + v
+        dx = round(2.0 + 2.0 * ((seed * 0.6180339887498949) % 1.0), 3)
+        out.append((seed, ag.random_spec(seed, dx=dx), (1.5, 3.0, 6.0)[seed % 3], dx))
+    return out
+
+
+def study_batch(n: int = 64, storage: str = "f16", quiet: bool = False):
+    """Batched variants: every seeded airbox alone in float32 (the reference's method, one solve at a
+    time), alone in `storage`, and all together in one batched run (tuned shape, one launch per step).
+    Reports aggregate MLUPS of each and each variant's KPI error against its float32 run."""
+    from airboxcalc_gb300 import airboxgen as ag
+    from airboxcalc_gb300 import batch as BT
+    from airboxcalc_gb300 import engine as E
+    geoms, params, rows, skipped = [], [], [], []
+    t32 = t16 = 0.0
+    cells = 0
+    for seed, spec, K, dx in batch_variants(n):
+        run = dict(RUN, K=K)
+        try:
+            g = E.prepare({"tris": ag.build_airbox(spec), **spec.prepare_params(), "maxCells": 1e10})
+            S = E.Simulation(g, run)
+            S.set_timing(True)
+            S.run()
+            ref = S.evaluate()["metrics"]
+        except E.AirboxError as e:
+            skipped.append({"seed": seed, "dx": dx, "code": e.code})
+            continue
+        t = S.timing()
+        t32 += t["run_ms"]
+        S16 = E.Simulation(g, dict(run, storage=storage))
+        S16.set_timing(True)
+        S16.run()
+        t16 += S16.timing()["run_ms"]
+        del S, S16
+        geoms.append(g)
+        params.append(dict(run, storage=storage))
+        rows.append({"seed": seed, "dx": dx, "K": K, "NF": g.nf, "ref": ref})
+        cells += g.nf
+    B = BT.Batch(geoms, params)
+    tuning = B.tune()
+    B.run()
+    B.reset()
+    st = B.run()
+    info = B.info
+    errs = []
+    for r, v, s_ in zip(rows, B.variants, st):
+        m = v.evaluate()["metrics"]
+        eg, ez = _rel_err(m, r["ref"])
+        errs.append(max(eg, ez))
+        r.update({"err_gammaCore": float(f"{eg:.3e}"), "err_zeta": float(f"{ez:.3e}"), "unstable_step": int(s_)})
+        del r["ref"]
+        if not quiet:
+            print(json.dumps(r), flush=True)
+    upd = cells * RUN["steps"]
+    out = {"study": "batch", "variants": len(rows), "skipped_unstable_or_leaking": len(skipped),
+           "cells_min": min(r["NF"] for r in rows), "cells_max": max(r["NF"] for r in rows), "cells_total": cells,
+           "storage": storage, "steps": RUN["steps"], "avg": RUN["avg"],
+           "batched_mlups": round(upd / (info["run_ms"] * 1e-3) / 1e6, 1),
+           "one_at_a_time_mlups": {storage: round(upd / (t16 * 1e-3) / 1e6, 1), "f32": round(upd / (t32 * 1e-3) / 1e6, 1)},
+           "batched_run_ms": round(info["run_ms"], 1), "kernel_launches": info["kernel_launches"],
+           "tuning": {k: tuning[k] for k in ("shape", "spw", "min_blocks", "grid", "ntiles", "ms_per_step")},
+           "tuning_candidates": tuning["candidates"],
+           "kpi_err_vs_individual_f32": {"max": float(f"{max(errs):.3e}"),
+                                         "median": float(f"{statistics.median(errs):.3e}"),
+                                         "within_0.5pct": round(sum(e < 0.005 for e in errs) / len(errs), 3),
+                                         "within_1pct": round(sum(e < 0.01 for e in errs) / len(errs), 3)}}
+    print(json.dumps(out), flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -270,8 +447,11 @@ def main():
     ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--study", choices=["precision", "converge"], default=None,
-                    help="instead of the bench line: KPI error per storage vs float64, or steps/time to converged KPIs")
+    ap.add_argument("--study", choices=["precision", "converge", "warmstart", "batch"], default=None,
+                    help="instead of the bench line: KPI error per storage vs float64, steps/time to converged "
+                         "KPIs, or the learned warm start on held-out airboxes")
+    ap.add_argument("--seeds", default="6000:6200", help="held-out seed range a:b of --study warmstart")
+    ap.add_argument("--weights", default=None, help="warm-start network weights (.npz)")
     a = ap.parse_args()
     ws, rank, local = dist_env()
     spec, run, desc = workload(a.workload)
@@ -280,6 +460,14 @@ def main():
         return 0
     if a.study == "converge":
         study_converge(spec, run, desc)
+        return 0
+    if a.study == "batch":
+        study_batch(64, a.storage if a.storage != "f32" else "f16")
+        return 0
+    if a.study == "warmstart":
+        from airboxcalc_gb300 import warmstart as W
+        lo, hi = map(int, a.seeds.split(":"))
+        study_warmstart(range(lo, hi), a.weights or W.WEIGHTS)
         return 0
 
     if a.impl == "reference":

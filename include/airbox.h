@@ -176,6 +176,38 @@ typedef struct {
   double gamma, gammaCore, lowCore, highCore, reverse, maxToMean, zeta, inlet_cm2, filter_cm2;
   double wm, cm; int n, cn, pinN, pbN, jb;
 } abx_metrics;
+/* field3d (src/engine.js:698-719) on the device: on every cell of the grid
+ * (index (i*ny + j)*nz + k; NaN where there is no air or k < kB) the speed
+ * |u|/u0, the static pressure relative to the space under the filter and
+ * the total-pressure loss since the inlet, both over q = u0^2/2.  Any of the
+ * three outputs may be NULL. */
+typedef struct {
+  int nx, ny, nz, kB, jm, top;
+  double h, x0, d0, z0, zIn, pleat;
+  double pin, rho_ref;        /* reference total pressure at the inlet, mean density on layer jb */
+} abx_field3d_info;
+int abx_sim_field3d(abx_sim *s, float *spd, float *pst, float *loss, abx_field3d_info *info);
+
+/* The cut planes of evaluate (src/engine.js:662-680): out holds planInlet
+ * (speed, ua = ux/u0, ub = uz/u0; nx*nz floats each, index i*nz + k), planLow
+ * (same layout) and lon (speed, ua = uz/u0, ub = uy/u0; nz*ny floats each,
+ * index k*ny + j): 6*nx*nz + 3*nz*ny floats. */
+typedef struct {
+  int ic, jc, jlow, n1, n2, lon_n1, lon_n2;
+  double depth_inlet, depth_low, x_lon;
+} abx_planes_info;
+int abx_sim_planes(abx_sim *s, float *out, abx_planes_info *info);
+
+/* streamlines (src/engine.js:721-758) traced on the device, one thread per
+ * seed: pts (3 floats per point, model coordinates), spd (|u|/u0 per point),
+ * off (n_lines + 1 prefix counts).  With capacities too small (e.g. 0) the
+ * counts are still reported and ABX_ERR_INVALID_ARGUMENT is returned. */
+typedef struct {
+  int seeds_opening, seeds_traced, n_lines, n_points;
+} abx_lines_info;
+int abx_sim_streamlines(abx_sim *s, int max_seeds, float *pts, float *spd, uint32_t *off, size_t cap_points,
+                        size_t cap_lines, abx_lines_info *info);
+
 /* evaluate() (src/engine.js:632-691) on the device: filter map at layer jm,
  * gamma, gamma core, lowCore, highCore, reverse, maxToMean and zeta, with
  * float64 sums.  fmap (nx*nz floats, w/mean or NaN) and hist (3 doubles
@@ -302,21 +334,23 @@ int abx_net_predict(abx_net *n, abx_sim *s, float *features, float *pred);
 int abx_sim_warm_start(abx_sim *s, abx_net *n);
 
 typedef struct {
-  int window;               /* steps per averaging window */
-  int min_windows;          /* windows before the stop rule may fire (>= 2) */
-  int max_steps;            /* give up after this many steps */
-  double tol;               /* stop when gamma core and zeta of two consecutive windows agree within tol (relative) */
+  int settle;               /* steps before averaging starts */
+  int window;               /* steps between checks of the running average */
+  int min_avg;              /* averaged steps before the stop rule may fire */
+  int max_steps;            /* give up after this many steps (settle included) */
+  double tol;               /* stop when gamma core and zeta of the running average moved less than tol
+                               (relative) over the last window */
 } abx_converge_params;
 
 typedef struct {
-  abx_metrics metrics;      /* evaluate() of the last window's averages */
+  abx_metrics metrics;      /* evaluate() of the running average at the stop */
   int steps, windows, converged;
-  double change;            /* last window-to-window relative change */
+  double change;            /* last window's relative change of the running average's KPIs */
 } abx_converge_result;
 
-/* Windowed run from the current state: averaging windows of `window` steps
- * until the stop rule fires or max_steps.  Non-finite KPIs end the run with
- * ABX_ERR_UNSTABLE. */
+/* Convergence run from the current state: `settle` steps, then steps added to
+ * a running average, evaluated every `window` steps, until the stop rule
+ * fires or max_steps.  Non-finite KPIs end the run with ABX_ERR_UNSTABLE. */
 int abx_sim_converge(abx_sim *s, const abx_converge_params *p, abx_converge_result *r);
 
 typedef struct {
@@ -331,6 +365,65 @@ typedef struct {
  * not converge within max_steps (or goes unstable) the simulation is reset to
  * f = w_i and runs the reference's steps/avg schedule (abx_sim_run). */
 int abx_sim_solve_warm(abx_sim *s, abx_net *n, const abx_converge_params *p, abx_warm_result *r);
+
+/* ======================================================================
+ * Batched variants: many simulations of different airboxes (uneven sizes,
+ * their own K / aniso / u / tau) advanced together, one kernel launch per
+ * LBM step over a tile list covering every variant, the steps captured in
+ * CUDA graphs.  The reference batches only variants sharing one geometry
+ * (GpuSim, src/engine.js:495-545, one lbm_step dispatch over B copies);
+ * here the geometries differ too.  Storage: float32, float16 or bfloat16;
+ * all variants share steps / avg / every and the storage.
+ * ====================================================================== */
+typedef struct abx_batch abx_batch;
+
+int abx_batch_create(abx_geom *const *geoms, const abx_run_params *params, int n, abx_batch **out);
+void abx_batch_free(abx_batch *b);
+
+/* Variant i as a simulation handle owned by the batch (do not free it):
+ * abx_sim_evaluate / abx_sim_get_acc / abx_sim_get_f read its state. */
+int abx_batch_sim(abx_batch *b, int i, abx_sim **out);
+
+/* Block shape of the batched step kernel: shape 0..2 (segments per warp 1/1/2,
+ * registers sized for 4/3/2 resident blocks per SM) and the grid (>= the
+ * number of tiles: one tile per block; fewer: blocks loop over the tiles). */
+typedef struct {
+  int shape, spw, min_blocks;
+  unsigned grid, ntiles;
+  double ms_per_step;            /* of the chosen shape, from the tuning run */
+  int n_candidates;
+  int cand_shape[32];
+  unsigned cand_grid[32];
+  double cand_ms[32];            /* time per LBM step of every candidate tried */
+} abx_batch_tuning;
+
+/* Autotuner: times a few steps of every candidate shape x grid on this
+ * batch's own domains, keeps the fastest, and resets every variant to
+ * f = w_i (the timed steps are discarded). */
+int abx_batch_tune(abx_batch *b, abx_batch_tuning *out);
+int abx_batch_set_shape(abx_batch *b, int shape, unsigned grid);
+
+/* Every variant back to f = w_i (averages and history cleared). */
+int abx_batch_reset(abx_batch *b);
+
+/* simulate()'s step loop (src/engine.js:341-358) for all variants at once:
+ * averaging window, a progress probe of every variant at each multiple of
+ * `every`.  A variant that goes unstable stops stepping (its evaluate then
+ * reports nothing new); the others go on.  status (n ints, may be NULL)
+ * receives 0 or the step where variant i went unstable. */
+int abx_batch_run(abx_batch *b, int *status);
+
+typedef struct {
+  int n;                          /* variants */
+  long long cells;                /* fluid cells over all variants */
+  long long state_bytes;
+  unsigned ntiles1, ntiles2;      /* tiles of 8 and 16 segments */
+  int shape;
+  unsigned grid;
+  double run_ms;                  /* device time of the last abx_batch_run */
+  long long kernel_launches;      /* of the last abx_batch_run */
+} abx_batch_info;
+int abx_batch_get_info(const abx_batch *b, abx_batch_info *out);
 
 #ifdef __cplusplus
 }

@@ -88,6 +88,17 @@ void ora_evaluate_f32(const ora_geom *g, const ora_sim *S, double u0, const floa
 void ora_evaluate_f64(const ora_geom *g, const ora_sim *S, double u0, const double *acc,
                       const float *ns, ora_metrics *m, float *fmap);
 
+/* post-processing of the averages (engine_ref_post.c) */
+double ora_js_hypot3(double x, double y, double z);
+double ora_js_round(double x);
+void ora_field3d(const ora_geom *g, const ora_sim *S, double u0, const float *acc, const float *ns, float *spd,
+                 float *pst, float *loss, int *kB_out, double *pin_out, double *rho_ref_out);
+void ora_planes(const ora_geom *g, const ora_sim *S, double u0, const float *acc, const float *ns, float *out,
+                int meta[3]);
+int ora_streamlines(const ora_geom *g, const ora_sim *S, double u0, const float *acc, const float *ns, int max_seeds,
+                    float *pts, float *spd, uint32_t *off, int cap_pts, int cap_lines, int *nlines_out,
+                    int *npts_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libengine_ref.so")
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
-    src = [os.path.join(HERE, f) for f in ("engine_ref.c", "engine_ref_step.inc", "engine_ref.h")]
+    src = [os.path.join(HERE, f) for f in ("engine_ref.c", "engine_ref_post.c", "engine_ref_step.inc", "engine_ref.h")]
     if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in src):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
@@ -99,6 +99,13 @@ def lib():
                                        C.POINTER(C.c_int), C.c_char_p]
         for nm in ("ora_evaluate_f32", "ora_evaluate_f64"):
             getattr(L, nm).argtypes = [C.POINTER(Geom), C.POINTER(Sim), C.c_double, fp, fp, C.POINTER(Metrics), fp]
+        L.ora_js_hypot3.restype = C.c_double
+        L.ora_js_hypot3.argtypes = [C.c_double] * 3
+        L.ora_field3d.argtypes = [C.POINTER(Geom), C.POINTER(Sim), C.c_double, fp, fp, fp, fp, fp,
+                                  C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.ora_planes.argtypes = [C.POINTER(Geom), C.POINTER(Sim), C.c_double, fp, fp, fp, C.c_int * 3]
+        L.ora_streamlines.argtypes = [C.POINTER(Geom), C.POINTER(Sim), C.c_double, fp, fp, C.c_int, fp, fp, fp,
+                                      C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         _lib = L
     return _lib
 
@@ -241,6 +248,36 @@ class OracleSim:
         if rc:
             raise OracleError(rc, msg.value.decode())
         return acc, hist[:3 * nh.value].reshape(-1, 3)
+
+    def field3d(self, acc, ns=None):
+        """field3d (src/engine.js:698-719) of float32 averages: spd, pst, loss (nx, ny, nz) and kB, pin, rhoRef."""
+        N = self.og.nx * self.og.ny * self.og.nz
+        out = [np.empty(N, np.float32) for _ in range(3)]
+        kB, pin, rr = C.c_int(), C.c_double(), C.c_double()
+        lib().ora_field3d(C.byref(self.og.g), C.byref(self.S), self.u0, _ptr(acc), _ptr(ns), *(_ptr(o) for o in out),
+                          C.byref(kB), C.byref(pin), C.byref(rr))
+        sh = (self.og.nx, self.og.ny, self.og.nz)
+        return [o.reshape(sh) for o in out], kB.value, pin.value, rr.value
+
+    def planes(self, acc, ns=None):
+        """evaluate's cut planes (src/engine.js:662-680): one float32 buffer and (ic, jc, jlow)."""
+        nx, ny, nz = self.og.nx, self.og.ny, self.og.nz
+        out = np.empty(6 * nx * nz + 3 * nz * ny, np.float32)
+        meta = (C.c_int * 3)()
+        lib().ora_planes(C.byref(self.og.g), C.byref(self.S), self.u0, _ptr(acc), _ptr(ns), _ptr(out), meta)
+        return out, tuple(meta)
+
+    def streamlines(self, acc, ns=None, max_seeds=220):
+        """streamlines (src/engine.js:721-758): pts (model coordinates), spd, off."""
+        cap_pts, cap_lines = 2100 * max(max_seeds, 1), max_seeds + 2
+        pts = np.empty(3 * cap_pts, np.float32)
+        spd = np.empty(cap_pts, np.float32)
+        off = np.empty(cap_lines, np.uint32)
+        nl, npt = C.c_int(), C.c_int()
+        rc = lib().ora_streamlines(C.byref(self.og.g), C.byref(self.S), self.u0, _ptr(acc), _ptr(ns), max_seeds,
+                                   _ptr(pts), _ptr(spd), _ptr(off), cap_pts, cap_lines, C.byref(nl), C.byref(npt))
+        assert rc == 0
+        return pts[:3 * npt.value], spd[:npt.value], off[:nl.value + 1]
 
     def evaluate(self, acc, ns=None):
         m = Metrics()

@@ -119,7 +119,7 @@ def targets(cls: np.ndarray, avg: dict, R: int, u0: float):
         for c, k in enumerate(("ux", "uy", "uz", "rho")):
             t[c] = _box_sums(np.where(fl > 0, avg[k], 0.0).astype(np.float64), R) / nf
     t[:3] /= u0
-    t[3] = (t[3] - 1.0) / (15 * u0 * u0)
+    t[3] = (t[3] - 1.0) / (5 * u0 * u0)
     t[:, nf == 0] = 0
     return t, nf / n
 
@@ -193,7 +193,7 @@ def apply(pred: np.ndarray, fluid: np.ndarray, ijk: np.ndarray, grid, u0: float)
     near = tuple(np.clip(np.rint(v).astype(np.int64), 0, R - 1) for v in f)
     p = np.where(wsum > 1e-6, p, pred[(slice(None),) + near])
     ux, uy, uz = p[0] * u0, p[1] * u0, p[2] * u0
-    rho = np.clip(1 + 15 * u0 * u0 * p[3], 0.9, 1.1)
+    rho = np.clip(1 + 5 * u0 * u0 * p[3], 0.9, 1.1)
     sp = np.sqrt(ux * ux + uy * uy + uz * uz)
     r = np.where(sp > 0.2, 0.2 / np.maximum(sp, 1e-300), 1.0)
     ux, uy, uz = ux * r, uy * r, uz * r

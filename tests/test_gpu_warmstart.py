@@ -143,13 +143,13 @@ def test_converge_and_fallback_to_the_reference_schedule():
     net = W.Net(16, 8, 2, seed=5)
     S = E.Simulation(g, RUN)
     W.warm_start(S, net)
-    r = W.converge(S, window=20, min_windows=2, max_steps=400, tol=0.5)
-    assert r["converged"] and r["steps"] % 20 == 0 and r["windows"] >= 2
+    r = W.converge(S, settle=20, window=20, min_avg=40, max_steps=400, tol=0.5)
+    assert r["converged"] and r["steps"] % 20 == 0 and r["windows"] >= 2 and r["steps"] >= 60
     assert all(np.isfinite(v) for v in r["metrics"].values())
     # a stop rule that cannot fire: the run falls back to f = w_i and the full schedule
     S2 = E.Simulation(g, RUN)
-    res = W.solve_warm(S2, net, window=20, min_windows=2, max_steps=40, tol=1e-14)
-    assert res["fell_back"] and res["warm_steps"] == 40 and res["steps"] == RUN["steps"]
+    res = W.solve_warm(S2, net, settle=10, window=20, min_avg=20, max_steps=50, tol=1e-14)
+    assert res["fell_back"] and res["warm_steps"] == 50 and res["steps"] == RUN["steps"]
     plain = E.simulate(g, RUN)["metrics"]
     for k in ("gamma", "gammaCore", "zeta", "maxToMean"):
         assert res["metrics"][k] == plain[k], k
