@@ -31,7 +31,7 @@ EXPORTS = [
     "abx_net_add_sample", "abx_net_clear_samples", "abx_net_get_sample", "abx_net_train", "abx_net_eval_loss",
     "abx_net_forward_backward", "abx_net_predict", "abx_sim_warm_start", "abx_sim_converge", "abx_sim_solve_warm",
     "abx_batch_create", "abx_batch_free", "abx_batch_sim", "abx_batch_tune", "abx_batch_set_shape", "abx_batch_reset",
-    "abx_batch_run", "abx_batch_get_info", "abx_sim_field3d", "abx_sim_planes", "abx_sim_streamlines",
+    "abx_batch_run", "abx_batch_get_info", "abx_batch_set_grouping", "abx_sim_field3d", "abx_sim_planes", "abx_sim_streamlines",
 ]
 
 
@@ -134,14 +134,16 @@ class LinesInfo(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("shape", C.c_int), ("spw", C.c_int), ("min_blocks", C.c_int), ("grid", C.c_uint),
-                ("ntiles", C.c_uint), ("ms_per_step", C.c_double), ("n_candidates", C.c_int),
-                ("cand_shape", C.c_int * 32), ("cand_grid", C.c_uint * 32), ("cand_ms", C.c_double * 32)]
+                ("ntiles", C.c_uint), ("ms_per_step", C.c_double), ("group_bytes", C.c_double),
+                ("n_groups", C.c_int), ("n_candidates", C.c_int),
+                ("cand_shape", C.c_int * 48), ("cand_grid", C.c_uint * 48), ("cand_group_bytes", C.c_double * 48),
+                ("cand_groups", C.c_int * 48), ("cand_ms", C.c_double * 48)]
 
 
 class BatchInfo(C.Structure):
     _fields_ = [("n", C.c_int), ("cells", C.c_longlong), ("state_bytes", C.c_longlong), ("ntiles1", C.c_uint),
                 ("ntiles2", C.c_uint), ("shape", C.c_int), ("grid", C.c_uint), ("run_ms", C.c_double),
-                ("kernel_launches", C.c_longlong)]
+                ("kernel_launches", C.c_longlong), ("n_groups", C.c_int), ("group_bytes", C.c_double)]
 
 
 _lib = None
@@ -212,6 +214,7 @@ def load(build_if_missing: bool = True):
     L.abx_batch_sim.argtypes = [vp, C.c_int, C.POINTER(vp)]
     L.abx_batch_tune.argtypes = [vp, C.POINTER(BatchTuning)]
     L.abx_batch_set_shape.argtypes = [vp, C.c_int, C.c_uint]
+    L.abx_batch_set_grouping.argtypes = [vp, C.c_double]
     L.abx_batch_reset.argtypes = [vp]
     L.abx_batch_run.argtypes = [vp, vp]
     L.abx_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]

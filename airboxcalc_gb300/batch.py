@@ -52,10 +52,15 @@ class Batch:
     def tune(self) -> dict:
         t = A.BatchTuning()
         E._check(A.load().abx_batch_tune(self._h, C.byref(t)))
-        cands = [{"shape": t.cand_shape[i], "grid": t.cand_grid[i], "ms_per_step": round(t.cand_ms[i], 4)}
-                 for i in range(t.n_candidates)]
+        cands = [{"shape": t.cand_shape[i], "grid": t.cand_grid[i], "group_mb": round(t.cand_group_bytes[i] / 1e6, 1),
+                  "groups": t.cand_groups[i], "ms_per_step": round(t.cand_ms[i], 4)} for i in range(t.n_candidates)]
         return {"shape": t.shape, "spw": t.spw, "min_blocks": t.min_blocks, "grid": t.grid, "ntiles": t.ntiles,
-                "ms_per_step": t.ms_per_step, "candidates": cands}
+                "ms_per_step": t.ms_per_step, "group_mb": round(t.group_bytes / 1e6, 1), "groups": t.n_groups,
+                "candidates": cands}
+
+    def set_grouping(self, group_bytes: float):
+        """Groups of variants of at most group_bytes of state each (0: no byte limit)."""
+        E._check(A.load().abx_batch_set_grouping(self._h, float(group_bytes)))
 
     def set_shape(self, shape: int, grid: int):
         E._check(A.load().abx_batch_set_shape(self._h, shape, grid))

@@ -1338,7 +1338,13 @@ struct abx_batch {
   std::vector<abx_sim *> sims;       // owned
   int storage = 0, steps = 0, avg = 0, every = 1;
   cudaStream_t st = nullptr;
-  StepArgs *d_vars = nullptr;
+  // Variants run in groups: consecutive variants whose state fits `group_bytes` (and at most kBatchChunk
+  // of them).  A chunk of steps runs group by group, each group for the whole chunk, so a group's state
+  // can stay in L2 across its steps; one launch per step and group, arguments by value.
+  double group_bytes = 0;                    // 0: one group of up to kBatchChunk variants after another
+  std::vector<BatchParams> chunks;           // one per group
+  std::vector<uint32_t> cstart[2];           // per spw: first tile of group c (and the end as last entry)
+  std::vector<uint2> tiles[2];               // host copy (variant-major)
   uint2 *d_tiles[2] = {nullptr, nullptr};   // tiles of 8 (spw 1) and 16 (spw 2) segments
   uint32_t ntiles[2] = {0, 0};
   int shape = 0;
@@ -1351,14 +1357,69 @@ struct abx_batch {
   ~abx_batch() {
     cudaSetDevice(device);
     if (st) cudaStreamSynchronize(st);
-    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    drop_graphs();
     for (auto e : ev) if (e) cudaEventDestroy(e);
-    cudaFree(d_vars); cudaFree(d_tiles[0]); cudaFree(d_tiles[1]);
+    cudaFree(d_tiles[0]); cudaFree(d_tiles[1]);
     for (auto *s : sims) delete s;
     if (st) cudaStreamDestroy(st);
   }
+  void drop_graphs() {
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+  }
+  static double state_bytes(const abx_sim *s) {
+    return (double)s->g->Np * (store_bytes(s->p.storage) * 19 + 4 + acc_bytes(s->p.storage) * 4);
+  }
+  // Split the variants into groups of at most `bytes` of state (bytes <= 0: no limit)
+  void regroup(double bytes) {
+    group_bytes = bytes;
+    chunks.clear();
+    cstart[0].clear(); cstart[1].clear();
+    std::vector<uint32_t> first_tile[2];
+    for (int k = 0; k < 2; k++) { first_tile[k].assign(n + 1, 0); }
+    for (int k = 0; k < 2; k++) {
+      uint32_t v = 0;
+      for (uint32_t t = 0; t <= tiles[k].size(); t++) {
+        const uint32_t tv = t < tiles[k].size() ? tiles[k][t].x : (uint32_t)n;
+        while (v <= tv && v <= (uint32_t)n) first_tile[k][v++] = t;
+      }
+    }
+    double acc_bytes_ = 0;
+    for (int i = 0; i < n; i++) {
+      const double sb = state_bytes(sims[i]);
+      const bool start = chunks.empty() || (int)(i - chunks.back().vbase) >= kBatchChunk ||
+                         (bytes > 0 && acc_bytes_ + sb > bytes);
+      if (start) {
+        chunks.emplace_back();
+        BatchParams &P = chunks.back();
+        std::memset(&P, 0, sizeof P);
+        P.vbase = (uint32_t)i;
+        acc_bytes_ = 0;
+        for (int k = 0; k < 2; k++) cstart[k].push_back(first_tile[k][i]);
+      }
+      chunks.back().v[i - chunks.back().vbase] = step_args(*sims[i]);
+      acc_bytes_ += sb;
+    }
+    for (int k = 0; k < 2; k++) cstart[k].push_back((uint32_t)tiles[k].size());
+    drop_graphs();
+  }
   uint32_t tiles_of(int sh) const { return ntiles[batch_shape_spw(sh) - 1]; }
   const uint2 *tile_ptr(int sh) const { return d_tiles[batch_shape_spw(sh) - 1]; }
+  // nsteps steps of every group, group by group, starting in form `form0`
+  cudaError_t launch(int nsteps, int form0, bool acc, int sh, uint32_t grid_) const {
+    const std::vector<uint32_t> &cs = cstart[batch_shape_spw(sh) - 1];
+    for (size_t c = 0; c < chunks.size(); c++) {
+      const uint32_t t0 = cs[c], t1 = cs[c + 1];
+      if (t1 <= t0) continue;
+      int form = form0;
+      for (int i = 0; i < nsteps; i++, form ^= 1) {
+        cudaError_t e = launch_step_batch(storage, form == 0, acc, sh, chunks[c], tile_ptr(sh), t0, t1,
+                                          std::min(grid_, t1 - t0), st);
+        if (e != cudaSuccess) return e;
+      }
+    }
+    return cudaSuccess;
+  }
 };
 
 extern "C" int abx_batch_create(abx_geom *const *geoms, const abx_run_params *params, int n, abx_batch **out) {
@@ -1390,16 +1451,13 @@ extern "C" int abx_batch_create(abx_geom *const *geoms, const abx_run_params *pa
   CK(cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking), "batch_create: stream");
   CK(cudaEventCreate(&b.ev[0]), "batch_create: events");
   CK(cudaEventCreate(&b.ev[1]), "batch_create: events");
-  std::vector<StepArgs> vars(n);
-  std::vector<uint2> tiles[2];
+  std::vector<uint2> (&tiles)[2] = b.tiles;
   for (int i = 0; i < n; i++) {
-    vars[i] = step_args(*b.sims[i]);
     const uint32_t nseg = b.sims[i]->g->nseg;
     for (int k = 0; k < 2; k++)
       for (uint32_t s0 = 0; s0 < nseg; s0 += 8u * (k + 1)) tiles[k].push_back(seg2((unsigned)i, s0));
   }
-  CK(cudaMalloc((void **)&b.d_vars, sizeof(StepArgs) * n), "batch_create: variants");
-  CK(cudaMemcpyAsync(b.d_vars, vars.data(), sizeof(StepArgs) * n, cudaMemcpyHostToDevice, b.st), "batch_create");
+  b.regroup(0);
   for (int k = 0; k < 2; k++) {
     b.ntiles[k] = (uint32_t)tiles[k].size();
     CK(cudaMalloc((void **)&b.d_tiles[k], sizeof(uint2) * std::max<size_t>(tiles[k].size(), 1)), "batch_create: tiles");
@@ -1445,13 +1503,7 @@ static int batch_steps(abx_batch *b, int n, bool acc) {
   if (it == b->graphs.end()) {
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal), "batch: capture");
-    cudaError_t le = cudaSuccess;
-    int form = b->form;
-    for (int i = 0; i < n && le == cudaSuccess; i++) {
-      le = launch_step_batch(b->storage, form == 0, acc, b->shape, b->d_vars, b->tile_ptr(b->shape), b->tiles_of(b->shape),
-                             b->grid, b->st);
-      form ^= 1;
-    }
+    const cudaError_t le = b->launch(n, b->form, acc, b->shape, b->grid);
     cudaError_t ce = cudaStreamEndCapture(b->st, &graph);
     if (le != cudaSuccess) { if (ce == cudaSuccess) cudaGraphDestroy(graph); return cuda_fail(le, "batch: step launch"); }
     CK(ce, "batch: capture");
@@ -1465,7 +1517,7 @@ static int batch_steps(abx_batch *b, int n, bool acc) {
   b->form ^= (n & 1);
   b->step += n;
   if (acc) b->nacc += n;
-  b->launches += n;
+  b->launches += (int64_t)n * (int64_t)b->chunks.size();
   return ABX_OK;
 }
 
@@ -1477,47 +1529,65 @@ extern "C" int abx_batch_set_shape(abx_batch *b, int shape, unsigned grid) {
   return ABX_OK;
 }
 
+extern "C" int abx_batch_set_grouping(abx_batch *b, double group_bytes) {
+  if (!b || !(group_bytes >= 0)) return fail(ABX_ERR_INVALID_ARGUMENT, "batch_set_grouping: group_bytes >= 0 required");
+  CK(cudaSetDevice(b->device), "batch_set_grouping");
+  CK(cudaStreamSynchronize(b->st), "batch_set_grouping");
+  b->regroup(group_bytes);
+  return ABX_OK;
+}
+
 extern "C" int abx_batch_tune(abx_batch *b, abx_batch_tuning *out) {
   clear_stale_error();
   if (!b || !out) return fail(ABX_ERR_INVALID_ARGUMENT, "batch_tune: null argument");
   CK(cudaSetDevice(b->device), "batch_tune");
   std::memset(out, 0, sizeof *out);
   if (int rc = abx_batch_reset(b)) return rc;
-  int nsm = 0;
+  int nsm = 0, l2 = 0;
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->device), "batch_tune");
-  constexpr int kReps = 6;  // odd+even step pairs timed per candidate
+  CK(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, b->device), "batch_tune");
+  // candidates: group budgets (none, and fractions of the L2) x block shapes x grids; each candidate times a
+  // sequence of steps per group, so that L2 reuse across a group's steps shows
+  constexpr int kSteps = 8;
+  const double budgets[4] = {0.0, 0.75 * l2, 0.5 * l2, 0.25 * l2};
   double best = INFINITY;
   int best_shape = 0;
   uint32_t best_grid = 1;
-  for (int sh = 0; sh < kBatchShapes; sh++) {
-    const uint32_t nt = b->tiles_of(sh);
-    if (nt == 0) continue;
-    const uint32_t mb = (uint32_t)batch_shape_minblocks(sh);
-    const uint32_t grids[4] = {nt, (uint32_t)nsm * mb, (uint32_t)nsm * mb * 2, (uint32_t)nsm * mb * 4};
-    for (int gi = 0; gi < 4; gi++) {
-      const uint32_t grid = std::min(grids[gi], nt);
-      bool dup = false;
-      for (int c = 0; c < out->n_candidates; c++) dup |= out->cand_shape[c] == sh && out->cand_grid[c] == grid;
-      if (dup || out->n_candidates >= 32) continue;
-      for (int w = 0; w < 2; w++)
-        CK(launch_step_batch(b->storage, (w & 1) == 0, false, sh, b->d_vars, b->tile_ptr(sh), nt, grid, b->st), "batch_tune");
-      CK(cudaEventRecord(b->ev[0], b->st), "batch_tune");
-      for (int r = 0; r < 2 * kReps; r++)
-        CK(launch_step_batch(b->storage, (r & 1) == 0, false, sh, b->d_vars, b->tile_ptr(sh), nt, grid, b->st), "batch_tune");
-      CK(cudaEventRecord(b->ev[1], b->st), "batch_tune");
-      CK(cudaEventSynchronize(b->ev[1]), "batch_tune");
-      float ms = 0;
-      CK(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]), "batch_tune");
-      const double per = ms / (2.0 * kReps);
-      const int c = out->n_candidates++;
-      out->cand_shape[c] = sh; out->cand_grid[c] = grid; out->cand_ms[c] = per;
-      if (per < best) { best = per; best_shape = sh; best_grid = grid; }
+  double best_budget = 0;
+  for (int bi = 0; bi < 4; bi++) {
+    b->regroup(budgets[bi]);
+    for (int sh = 0; sh < kBatchShapes; sh++) {
+      const uint32_t nt = b->tiles_of(sh);
+      if (nt == 0) continue;
+      const uint32_t mb = (uint32_t)batch_shape_minblocks(sh);
+      const uint32_t grids[3] = {(uint32_t)nsm * mb, (uint32_t)nsm * mb * 2, nt};
+      for (int gi = 0; gi < 3; gi++) {
+        const uint32_t grid = std::min(grids[gi], nt);
+        bool dup = false;
+        for (int c = 0; c < out->n_candidates; c++)
+          dup |= out->cand_shape[c] == sh && out->cand_grid[c] == grid && out->cand_group_bytes[c] == budgets[bi];
+        if (dup || out->n_candidates >= 48) continue;
+        CK(b->launch(2, 0, false, sh, grid), "batch_tune");
+        CK(cudaEventRecord(b->ev[0], b->st), "batch_tune");
+        CK(b->launch(kSteps, 0, false, sh, grid), "batch_tune");
+        CK(cudaEventRecord(b->ev[1], b->st), "batch_tune");
+        CK(cudaEventSynchronize(b->ev[1]), "batch_tune");
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]), "batch_tune");
+        const double per = ms / kSteps;
+        const int c = out->n_candidates++;
+        out->cand_shape[c] = sh; out->cand_grid[c] = grid; out->cand_ms[c] = per;
+        out->cand_group_bytes[c] = budgets[bi]; out->cand_groups[c] = (int)b->chunks.size();
+        if (per < best) { best = per; best_shape = sh; best_grid = grid; best_budget = budgets[bi]; }
+      }
     }
   }
+  b->regroup(best_budget);
   b->shape = best_shape;
   b->grid = best_grid;
   out->shape = best_shape; out->spw = batch_shape_spw(best_shape); out->min_blocks = batch_shape_minblocks(best_shape);
   out->grid = best_grid; out->ntiles = b->tiles_of(best_shape); out->ms_per_step = best;
+  out->group_bytes = best_budget; out->n_groups = (int)b->chunks.size();
   return abx_batch_reset(b);   // the tuning steps advanced the state: start over from f = w_i
 }
 
@@ -1577,6 +1647,7 @@ extern "C" int abx_batch_get_info(const abx_batch *b, abx_batch_info *o) {
   }
   o->ntiles1 = b->ntiles[0]; o->ntiles2 = b->ntiles[1];
   o->shape = b->shape; o->grid = b->grid; o->run_ms = b->run_ms; o->kernel_launches = b->launches;
+  o->n_groups = (int)b->chunks.size(); o->group_bytes = b->group_bytes;
   return ABX_OK;
 }
 

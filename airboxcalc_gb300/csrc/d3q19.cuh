@@ -158,7 +158,8 @@ __device__ __forceinline__ void collide(const L (&fi)[19], uint32_t cls, L nsv, 
   const L tau = (L)0.5 * (P.tau0 + sqrt(P.tau0 * P.tau0 + P.cs2s * Qn / rho));
   if (cls == kClsFilter) {
     const L a1 = tau * P.sig * P.aniso, a2 = tau * P.sig;
-    const L sl = (L)1 - (a1 < (L)0.9 ? a1 : (L)0.9), sv = (L)1 - (a2 < (L)0.9 ? a2 : (L)0.9);
+    // Math.min(a, 0.9): a NaN coefficient (e.g. sigma = 0/0 with zero inflow) propagates as in the reference
+    const L sl = (L)1 - (a1 >= (L)0.9 ? (L)0.9 : a1), sv = (L)1 - (a2 >= (L)0.9 ? (L)0.9 : a2);
     const L ex = ux * sl, ey = uy * sv, ez = uz * sl;
     usq = (L)1.5 * (ex * ex + ey * ey + ez * ez);
 #pragma unroll
@@ -232,7 +233,7 @@ __device__ __forceinline__ void collide_fast(const float (&f)[19], uint32_t cls,
     const float tau = 0.5f * (P.tau0 + sqrtf(P.tau0 * P.tau0 + P.cs2s * sqrtf(q2) * inv));
     if (cls == kClsFilter) {
       const float a1 = tau * P.sig * P.aniso, a2 = tau * P.sig;
-      const float sl = 1.0f - fminf(a1, 0.9f), sv = 1.0f - fminf(a2, 0.9f);
+      const float sl = 1.0f - (a1 >= 0.9f ? 0.9f : a1), sv = 1.0f - (a2 >= 0.9f ? 0.9f : a2);  // Math.min, NaN kept
       vx = ux * sl; vy = uy * sv; vz = uz * sl;
       ux = 0.5f * (ux + vx); uy = 0.5f * (uy + vy); uz = 0.5f * (uz + vz);
     }

@@ -34,26 +34,26 @@ static cudaError_t step_k(bool odd, bool acc, bool has_ns, const StepArgs &a, cu
 
 // ------------------------------------------------------------------ batched step (many domains)
 template <int K, int SPW, int MINB>
-static cudaError_t step_batch_k(bool odd, bool acc, const StepArgs *vars, const uint2 *tiles, uint32_t ntiles,
+static cudaError_t step_batch_k(bool odd, bool acc, const BatchParams &P, const uint2 *tiles, uint32_t t0, uint32_t t1,
                                 uint32_t grid, cudaStream_t st) {
-  if (ntiles == 0) return cudaSuccess;
+  if (t1 <= t0) return cudaSuccess;
   if (odd) {
-    if (acc) aa_step_batch_kernel<K, true, true, SPW, MINB><<<grid, 256, 0, st>>>(vars, tiles, ntiles);
-    else aa_step_batch_kernel<K, true, false, SPW, MINB><<<grid, 256, 0, st>>>(vars, tiles, ntiles);
+    if (acc) aa_step_batch_kernel<K, true, true, SPW, MINB><<<grid, 256, 0, st>>>(P, tiles, t0, t1);
+    else aa_step_batch_kernel<K, true, false, SPW, MINB><<<grid, 256, 0, st>>>(P, tiles, t0, t1);
   } else {
-    if (acc) aa_step_batch_kernel<K, false, true, SPW, MINB><<<grid, 256, 0, st>>>(vars, tiles, ntiles);
-    else aa_step_batch_kernel<K, false, false, SPW, MINB><<<grid, 256, 0, st>>>(vars, tiles, ntiles);
+    if (acc) aa_step_batch_kernel<K, false, true, SPW, MINB><<<grid, 256, 0, st>>>(P, tiles, t0, t1);
+    else aa_step_batch_kernel<K, false, false, SPW, MINB><<<grid, 256, 0, st>>>(P, tiles, t0, t1);
   }
   return cudaGetLastError();
 }
 
 template <int K>
-static cudaError_t step_batch_shape(int shape, bool odd, bool acc, const StepArgs *vars, const uint2 *tiles,
-                                    uint32_t ntiles, uint32_t grid, cudaStream_t st) {
+static cudaError_t step_batch_shape(int shape, bool odd, bool acc, const BatchParams &P, const uint2 *tiles,
+                                    uint32_t t0, uint32_t t1, uint32_t grid, cudaStream_t st) {
   switch (shape) {
-    case 0: return step_batch_k<K, 1, 4>(odd, acc, vars, tiles, ntiles, grid, st);
-    case 1: return step_batch_k<K, 1, 3>(odd, acc, vars, tiles, ntiles, grid, st);
-    case 2: return step_batch_k<K, 2, 2>(odd, acc, vars, tiles, ntiles, grid, st);
+    case 0: return step_batch_k<K, 1, 4>(odd, acc, P, tiles, t0, t1, grid, st);
+    case 1: return step_batch_k<K, 1, 3>(odd, acc, P, tiles, t0, t1, grid, st);
+    case 2: return step_batch_k<K, 2, 2>(odd, acc, P, tiles, t0, t1, grid, st);
   }
   return cudaErrorInvalidValue;
 }
@@ -61,13 +61,13 @@ static cudaError_t step_batch_shape(int shape, bool odd, bool acc, const StepArg
 int batch_shape_spw(int shape) { return shape == 2 ? 2 : 1; }
 int batch_shape_minblocks(int shape) { return shape == 0 ? 4 : shape == 1 ? 3 : 2; }
 
-cudaError_t launch_step_batch(int storage, bool odd, bool acc, int shape, const StepArgs *vars, const uint2 *tiles,
-                              uint32_t ntiles, uint32_t grid, cudaStream_t st) {
+cudaError_t launch_step_batch(int storage, bool odd, bool acc, int shape, const BatchParams &P, const uint2 *tiles,
+                              uint32_t t0, uint32_t t1, uint32_t grid, cudaStream_t st) {
   if (grid == 0 || shape < 0 || shape >= kBatchShapes) return cudaErrorInvalidValue;
   switch (storage) {
-    case kStoreF32: return step_batch_shape<kStoreF32>(shape, odd, acc, vars, tiles, ntiles, grid, st);
-    case kStoreF16: return step_batch_shape<kStoreF16>(shape, odd, acc, vars, tiles, ntiles, grid, st);
-    case kStoreBF16: return step_batch_shape<kStoreBF16>(shape, odd, acc, vars, tiles, ntiles, grid, st);
+    case kStoreF32: return step_batch_shape<kStoreF32>(shape, odd, acc, P, tiles, t0, t1, grid, st);
+    case kStoreF16: return step_batch_shape<kStoreF16>(shape, odd, acc, P, tiles, t0, t1, grid, st);
+    case kStoreBF16: return step_batch_shape<kStoreBF16>(shape, odd, acc, P, tiles, t0, t1, grid, st);
   }
   return cudaErrorInvalidValue;
 }

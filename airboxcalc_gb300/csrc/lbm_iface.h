@@ -84,15 +84,21 @@ cudaError_t launch_evaluate(int storage, const StateArgs &a, const EvalArgs &e, 
 cudaError_t launch_step_fast(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, const TmaBlob *tma,
                              cudaStream_t st);
 
-// One step of many domains in one launch (lbm_fast.cu; float32, float16, bfloat16 storage).
-// vars: device array of the domains' StepArgs; tiles[t] = {domain, first segment} of 8*spw segments;
-// grid blocks loop over the tiles (grid >= ntiles: one tile per block).  shape (0..kBatchShapes-1)
-// selects segments per warp (spw) and the resident blocks per SM the kernel's registers are sized for.
+// One step of many domains in one launch (lbm_fast.cu; float32, float16, bfloat16 storage).  Up to
+// kBatchChunk variants per launch, their StepArgs passed by value (kernel parameter); tiles[t] = {variant,
+// first segment} of 8*spw segments, variants vbase.. of the chunk in tiles [t0, t1); grid blocks loop over
+// the tiles (grid >= t1 - t0: one tile per block).  shape (0..kBatchShapes-1) selects segments per warp
+// (spw) and the resident blocks per SM the kernel's registers are sized for.
+constexpr int kBatchChunk = 96;
+struct BatchParams {
+  StepArgs v[kBatchChunk];
+  uint32_t vbase;
+};
 constexpr int kBatchShapes = 3;
 int batch_shape_spw(int shape);
 int batch_shape_minblocks(int shape);
-cudaError_t launch_step_batch(int storage, bool odd, bool acc, int shape, const StepArgs *vars, const uint2 *tiles,
-                              uint32_t ntiles, uint32_t grid, cudaStream_t st);
+cudaError_t launch_step_batch(int storage, bool odd, bool acc, int shape, const BatchParams &P, const uint2 *tiles,
+                              uint32_t t0, uint32_t t1, uint32_t grid, cudaStream_t st);
 
 // Mask construction (lbm_exact.cu): class bytes (0 not fluid, 1 bulk, 2 inlet,
 // 3 outlet, 4 filter; index (i*ny+j)*nz+k) -> padded mask words, cell (i,j,k)

@@ -127,28 +127,32 @@ __device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, cons
   }
 }
 
+// Traversal order: blocks run in rising index order, so a step ends with the last segments' lines in
+// L2.  Odd steps walk the segments backwards: each step starts where the previous one ended and reads
+// what is still in L2 (state up to about the L2's 129 MB stays on chip across steps).
+#ifndef ABX_STEP_ALTERNATE
+#define ABX_STEP_ALTERNATE 1
+#endif
+
 template <int K, bool ODD, bool ACC, bool HAS_NS>
 __global__ void __launch_bounds__(256, ABX_STEP_MINBLOCKS) aa_step_kernel(const StepArgs a) {
-  step_warp<K, ODD, ACC, HAS_NS, kStepSpw>(a, (blockIdx.x * 8u + (threadIdx.x >> 5)) * kStepSpw, threadIdx.x & 31);
+  const uint32_t blk = (ABX_STEP_ALTERNATE && ODD) ? gridDim.x - 1u - blockIdx.x : blockIdx.x;
+  step_warp<K, ODD, ACC, HAS_NS, kStepSpw>(a, (blk * 8u + (threadIdx.x >> 5)) * kStepSpw, threadIdx.x & 31);
 }
 
 // One step of many domains in one launch.  tiles[t] = {variant, first segment}: a block takes 8*SPW
-// consecutive segments of one variant; with fewer blocks than tiles the blocks loop over the tile list
-// (persistent).  The variant's arguments are staged in shared memory for the block.  SPW (segments
-// per warp) and MINB (resident blocks per SM the registers are sized for) are the autotuner's knobs.
+// consecutive segments of one variant; the blocks loop over tiles [t0, t1) (persistent when the grid is
+// smaller).  The variants' arguments travel as one kernel parameter (constant bank, read with the tile's
+// variant index), so the per-cell code is the single-domain kernel's.  SPW (segments per warp) and MINB
+// (resident blocks per SM the registers are sized for) are the autotuner's knobs.
 template <int K, bool ODD, bool ACC, int SPW, int MINB>
 __global__ void __launch_bounds__(256, MINB)
-    aa_step_batch_kernel(const StepArgs *__restrict__ vars, const uint2 *__restrict__ tiles, uint32_t ntiles) {
-  __shared__ __align__(16) StepArgs sa;
-  static_assert(sizeof(StepArgs) % 8 == 0 && sizeof(StepArgs) / 8 <= 256, "StepArgs staging");
-  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const uint2 tile = tiles[t];
-    __syncthreads();
-    if (threadIdx.x < sizeof(StepArgs) / 8)
-      reinterpret_cast<unsigned long long *>(&sa)[threadIdx.x] =
-          reinterpret_cast<const unsigned long long *>(vars + tile.x)[threadIdx.x];
-    __syncthreads();
-    step_warp<K, ODD, ACC, false, SPW>(sa, tile.y + (threadIdx.x >> 5) * SPW, threadIdx.x & 31);
+    aa_step_batch_kernel(const __grid_constant__ BatchParams P, const uint2 *__restrict__ tiles, uint32_t t0,
+                         uint32_t t1) {
+  const uint32_t n = t1 - t0;
+  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+    const uint2 tile = tiles[t0 + ((ABX_STEP_ALTERNATE && ODD) ? n - 1u - i : i)];
+    step_warp<K, ODD, ACC, false, SPW>(P.v[tile.x - P.vbase], tile.y + (threadIdx.x >> 5) * SPW, threadIdx.x & 31);
   }
 }
 

@@ -428,7 +428,8 @@ def study_batch(n: int = 64, storage: str = "f16", quiet: bool = False):
            "batched_mlups": round(upd / (info["run_ms"] * 1e-3) / 1e6, 1),
            "one_at_a_time_mlups": {storage: round(upd / (t16 * 1e-3) / 1e6, 1), "f32": round(upd / (t32 * 1e-3) / 1e6, 1)},
            "batched_run_ms": round(info["run_ms"], 1), "kernel_launches": info["kernel_launches"],
-           "tuning": {k: tuning[k] for k in ("shape", "spw", "min_blocks", "grid", "ntiles", "ms_per_step")},
+           "tuning": {k: tuning[k] for k in ("shape", "spw", "min_blocks", "grid", "ntiles", "ms_per_step", "group_mb",
+                                             "groups")},
            "tuning_candidates": tuning["candidates"],
            "kpi_err_vs_individual_f32": {"max": float(f"{max(errs):.3e}"),
                                          "median": float(f"{statistics.median(errs):.3e}"),

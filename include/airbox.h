@@ -390,16 +390,26 @@ int abx_batch_sim(abx_batch *b, int i, abx_sim **out);
 typedef struct {
   int shape, spw, min_blocks;
   unsigned grid, ntiles;
-  double ms_per_step;            /* of the chosen shape, from the tuning run */
+  double ms_per_step;            /* of the chosen candidate, from the tuning run */
+  double group_bytes;            /* chosen group budget (0: no limit) */
+  int n_groups;
   int n_candidates;
-  int cand_shape[32];
-  unsigned cand_grid[32];
-  double cand_ms[32];            /* time per LBM step of every candidate tried */
+  int cand_shape[48];
+  unsigned cand_grid[48];
+  double cand_group_bytes[48];
+  int cand_groups[48];
+  double cand_ms[48];            /* time per LBM step of every candidate tried */
 } abx_batch_tuning;
 
-/* Autotuner: times a few steps of every candidate shape x grid on this
- * batch's own domains, keeps the fastest, and resets every variant to
- * f = w_i (the timed steps are discarded). */
+/* Variants run in groups of consecutive variants whose state fits
+ * group_bytes (at most 96 per group; 0: no byte limit).  A chunk of steps
+ * runs group by group, each group for the whole chunk, so that a group that
+ * fits in L2 stays there across its steps. */
+int abx_batch_set_grouping(abx_batch *b, double group_bytes);
+
+/* Autotuner: times a few steps of every candidate group budget x shape x
+ * grid on this batch's own domains, keeps the fastest, and resets every
+ * variant to f = w_i (the timed steps are discarded). */
 int abx_batch_tune(abx_batch *b, abx_batch_tuning *out);
 int abx_batch_set_shape(abx_batch *b, int shape, unsigned grid);
 
@@ -422,6 +432,8 @@ typedef struct {
   unsigned grid;
   double run_ms;                  /* device time of the last abx_batch_run */
   long long kernel_launches;      /* of the last abx_batch_run */
+  int n_groups;
+  double group_bytes;
 } abx_batch_info;
 int abx_batch_get_info(const abx_batch *b, abx_batch_info *out);
 

@@ -22,12 +22,13 @@
 
 double ora_js_hypot3(double x, double y, double z) {
   const double a[3] = {fabs(x), fabs(y), fabs(z)};
+  /* ECMAScript Math.hypot: an infinite argument gives +Infinity even next to a NaN */
+  for (int i = 0; i < 3; i++) if (isinf(a[i])) return INFINITY;
   double mx = 0;
   for (int i = 0; i < 3; i++) {
     if (isnan(a[i])) return NAN;
     if (a[i] > mx) mx = a[i];
   }
-  if (isinf(mx)) return INFINITY;
   if (mx == 0) return 0;
   double sum = 0, comp = 0;
   for (int i = 0; i < 3; i++) {

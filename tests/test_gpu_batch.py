@@ -58,15 +58,16 @@ def test_shapes_and_grids_agree():
     params = [dict(p, storage="f16") for p in params]
     B = BT.Batch(geoms, params)
     out = []
-    for shape, grid in ((0, 10 ** 6), (1, 7), (2, 3)):
+    for shape, grid, group in ((0, 10 ** 6, 0), (1, 7, 0), (2, 3, 0), (0, 300, 1.0), (1, 5, 2e6)):
         B.reset()
+        B.set_grouping(group)           # 1 byte: every variant its own group
         B.set_shape(shape, grid)
         B.run()
+        assert B.info["n_groups"] == (3 if group == 1.0 else B.info["n_groups"])
         out.append([v.get_acc() for v in B.variants])
-    for a, b in zip(out[0], out[1]):
-        assert np.array_equal(a, b)
-    for a, b in zip(out[0], out[2]):
-        assert np.array_equal(a, b)
+    for o in out[1:]:
+        for a, b in zip(out[0], o):
+            assert np.array_equal(a, b)
 
 
 def test_unstable_variant_stops_alone():
@@ -86,3 +87,17 @@ def test_batch_argument_errors():
         BT.Batch(geoms, [params[0], dict(params[1], steps=60), params[2]])
     with pytest.raises(E.AirboxError):
         BT.Batch(geoms, [dict(p, storage="f64") for p in params])
+
+
+def test_batches_larger_than_one_launch():
+    """More variants than one launch carries (96): the steps are split over several launches."""
+    spec = ag.AirboxSpec(**SMALL)
+    g = E.prepare({"tris": ag.build_airbox(spec), **spec.prepare_params()})
+    run = dict(RUN, steps=60, avg=20, every=30, storage="f16")
+    params = [dict(run, K=1.0 + 0.05 * i) for i in range(100)]
+    B = BT.Batch([g] * 100, params)
+    B.tune()
+    assert not B.run().any()
+    for i in (0, 95, 96, 99):
+        _, ref_acc = individual(g, params[i])
+        assert np.array_equal(B.variants[i].get_acc(), ref_acc), i

@@ -246,6 +246,19 @@ def test_tma_pipeline_matches_direct_kernel(storage, monkeypatch):
         assert np.abs(aa - ab).max() < 1e-5
 
 
+@pytest.mark.parametrize("storage", ["f32exact", "f32", "f16", "bf16"])
+def test_zero_inflow_fails_like_the_reference(storage):
+    """u = 0 makes the filter coefficient 0/0 (src/engine.js:258): Math.min keeps the NaN, the fields go
+    non-finite and the first progress check reports the instability, as in the oracle."""
+    og, g = prep_both(ag.AirboxSpec(**SMALL))
+    run = dict(K=3.0, aniso=10.0, u=0.0, tau=0.51, steps=200, avg=50, every=50)
+    with pytest.raises(O.OracleError) as eo:
+        O.OracleSim(og, run).simulate(200, 50, 50, nthreads=NT)
+    with pytest.raises(E.AirboxError) as eg:
+        E.Simulation(g, {**run, "storage": storage}).run()
+    assert eg.value.code == 10 and str(eg.value) == str(eo.value)
+
+
 @pytest.mark.parametrize("storage", ["f32exact", "f32", "f16"])
 def test_instability_reported_like_the_reference(storage):
     """progressInfo's check (src/engine.js:334-335): a run that blows up fails
