@@ -45,7 +45,15 @@ template <int K> struct Store;
 template <> struct Store<kStoreF32> {
   using T = float; using L = float; using Acc = float;
   __device__ static __forceinline__ L lds(const T *p, L) { return *p; }
-#if ABX_CACHE_HINTS
+#if ABX_CACHE_HINTS == 2
+  // evict-first load that also asks L2 to fetch the surrounding 256-byte block
+  __device__ static __forceinline__ L ld(const T *p, L) {
+    float v;
+    asm volatile("ld.global.cs.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+  }
+  __device__ static __forceinline__ void st(T *p, L v, L) { __stcs(p, v); }
+#elif ABX_CACHE_HINTS
   __device__ static __forceinline__ L ld(const T *p, L) { return __ldcs(p); }
   __device__ static __forceinline__ void st(T *p, L v, L) { __stcs(p, v); }
 #else

@@ -448,6 +448,7 @@ def main():
     ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-warm-start", action="store_true", help="skip the warm-start sample of the bench line")
     ap.add_argument("--study", choices=["precision", "converge", "warmstart", "batch"], default=None,
                     help="instead of the bench line: KPI error per storage vs float64, steps/time to converged "
                          "KPIs, or the learned warm start on held-out airboxes")
@@ -606,6 +607,20 @@ def main():
         line["cpu_baseline"] = {"value": round(v, 3), "unit": "MLUPS", "cores": 1, "kind": "port",
                                 "sample": f"{n} LBM steps of the same airbox (NF={nf}) from w_i in {el:.1f} s, "
                                           "oracle restatement of src/engine.js cpuStep (float64 locals), 1 thread"}
+    if rank == 0 and not a.no_warm_start:
+        from airboxcalc_gb300 import warmstart as W
+        if os.path.exists(W.WEIGHTS):
+            summ, _ = study_warmstart(range(6000, 6012), W.WEIGHTS, rules=WARM_RULES[:1], uniform=False,
+                                      noise=False, quiet=True)
+            w = summ["warm0_f16"]
+            line["warm_start"] = {
+                "what": "time to converged gamma core / zeta: float16 + learned warm start + convergence run vs the "
+                        "plain float32 run (6000/2000 steps), host wall time per solve, held-out seeded airboxes "
+                        "6000-6011 at dx 2 mm (the full 200-seed study: bench.py --study warmstart)",
+                "airboxes": w["n"], "median_speedup_vs_plain_f32": w["median_speedup_vs_plain_f32"],
+                "within_1pct_both_kpis": w["within_1pct"], "median_err_gammaCore": w["median_err_gammaCore"],
+                "median_err_zeta": w["median_err_zeta"], "fallback_rate": w["fallback_rate"],
+                "median_steps": w["median_steps"], "rule": WARM_RULES[0]}
     if rank == 0:
         print(json.dumps(line))
     dist.close()
