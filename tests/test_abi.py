@@ -64,3 +64,21 @@ def test_compute_calls_fail_loudly_without_gpu():
     with pytest.raises(E.AirboxError) as ei:
         E.prepare({"tris": ag.build_airbox(spec), **spec.prepare_params()})
     assert ei.value.code == A.ERR_CUDA
+
+
+def test_warm_start_and_batch_entry_points_check_arguments_without_gpu():
+    """Argument checks answer before any CUDA call; valid calls fail loudly (no CPU fallback)."""
+    import ctypes as C
+    L = A.load()
+    h = C.c_void_p()
+    bad = A.NetParams(res=12, base=16, levels=4, device=0, seed=0)
+    assert L.abx_net_create(C.byref(bad), C.byref(h)) == A.ERR_INVALID_ARGUMENT
+    assert "power of two" in A.last_error()
+    bad = A.NetParams(res=64, base=12, levels=4, device=0, seed=0)
+    assert L.abx_net_create(C.byref(bad), C.byref(h)) == A.ERR_INVALID_ARGUMENT
+    ok = A.NetParams(res=64, base=16, levels=4, device=0, seed=0)
+    assert L.abx_net_create(C.byref(ok), C.byref(h)) == A.ERR_CUDA          # no GPU here
+    r = A.ConvergeResult()
+    assert L.abx_sim_converge(None, None, C.byref(r)) == A.ERR_INVALID_ARGUMENT
+    assert L.abx_batch_create(None, None, 0, C.byref(h)) == A.ERR_INVALID_ARGUMENT
+    assert L.abx_sim_streamlines(None, 220, None, None, None, 0, 0, None) == A.ERR_INVALID_ARGUMENT
