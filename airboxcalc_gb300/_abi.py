@@ -52,7 +52,8 @@ class GeomInfo(C.Structure):
                 ("pleat", C.c_double), ("volume_l", C.c_double), ("inlet_cm2", C.c_double),
                 ("filter_cm2", C.c_double), ("outlet_cm2", C.c_double), ("outlet_cm2_real", C.c_double),
                 ("frame_cy", C.c_double), ("frame_sy", C.c_double), ("kernel_launches", C.c_int64),
-                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64)]
+                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("ms_voxelize", C.c_double),
+                ("ms_masks", C.c_double), ("ms_device", C.c_double)]
 
 
 class RunParams(C.Structure):

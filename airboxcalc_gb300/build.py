@@ -7,6 +7,7 @@ Translation units, compiled in parallel:
   csrc/warmstart.cu  nvcc (grid <-> network resampling, warm-start initialisation)
   csrc/nn.cu         nvcc (layer kernels of the warm-start network, forward and backward)
   csrc/postproc.cu   nvcc, -fmad=false (field3d, cut planes, streamlines in the reference's float64 order)
+  csrc/prepare.cu    nvcc (duct, flood fill, leak, outlet, classes, kpad, segments, compact cell list)
   csrc/api.cpp       g++ -ffp-contract=off (host side of the C ABI)
   csrc/net.cpp       g++ (host side of the warm-start network: layers, training loop)
 and linked with nvcc -shared (static CUDA runtime).  No torch, no cmake.
@@ -36,6 +37,7 @@ UNITS = [
     ("warmstart.cu", []),
     ("nn.cu", []),
     ("postproc.cu", ["-fmad=false"]),
+    ("prepare.cu", []),
     ("api.cpp", None),
     ("net.cpp", None),
 ]

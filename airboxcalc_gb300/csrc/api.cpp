@@ -144,20 +144,23 @@ struct abx_geom {
   double h = 0, hf = 0, origin[3] = {0, 0, 0}, mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0}, pleat = 0;
   bool has_outlet = false;
   std::vector<float> tris_local, xc, dc, zc;
-  std::vector<uint8_t> solid, fluid, opening, outlet, cls;
+  std::vector<uint8_t> opening;      // nx*ny (host: the opening search runs on the host)
   // device-side, shared by the simulations of this geometry
+  uint8_t *d_solid = nullptr, *d_fluid = nullptr, *d_outlet = nullptr;   // N bytes each
   uint32_t *d_mask = nullptr;
   uint2 *d_seg = nullptr;
   uint32_t nseg = 0;
   int64_t kpad = 0;
   uint8_t *d_opening = nullptr;
   int64_t *d_cells = nullptr;       // padded index of each fluid cell, compact (c) order
-  std::vector<int64_t> cells_p;     // host copy
-  std::vector<int> cells_j;         // j of each fluid cell
+  std::vector<int64_t> layer_m, layer_t;   // padded indices of the air on layers jm and top+1, compact order
   int Ain = 0, Lp = 0;
   int64_t launches = 0, h2d = 0, d2h = 0;
+  double ms_vox = 0, ms_masks = 0, ms_device = 0;
   ~abx_geom() {
-    if (d_mask) { cudaSetDevice(device); cudaFree(d_mask); cudaFree(d_seg); cudaFree(d_opening); cudaFree(d_cells); }
+    cudaSetDevice(device);
+    cudaFree(d_solid); cudaFree(d_fluid); cudaFree(d_outlet);
+    cudaFree(d_mask); cudaFree(d_seg); cudaFree(d_opening); cudaFree(d_cells);
   }
 };
 
@@ -185,7 +188,8 @@ struct StreamHolder {
 }  // namespace
 
 // Opening search, duct, closing, flood, leak check and outlet (src/engine.js:141-216) on the host.
-static int finish_geometry(abx_geom &g, const abx_prepare_params *p, const std::vector<uint8_t> &slice) {
+static int finish_geometry(abx_geom &g, const abx_prepare_params *p, const std::vector<uint8_t> &slice,
+                           cudaStream_t st) {
   const int nx = g.nx, ny = g.ny, nz = g.nz, nxf = g.nxf, nyf = g.nyf;
   const double h = g.h, hf = g.hf;
   const int64_t nfs = (int64_t)nxf * nyf;
@@ -258,49 +262,50 @@ static int finish_geometry(abx_geom &g, const abx_prepare_params *p, const std::
   for (size_t c = 0; c < sel.size(); c++) if (sel[c] >= 5) { g.opening[c] = 1; g.nOpen++; }
   if (g.nOpen < 8) return fail(ABX_ERR_OPENING_TOO_SMALL, "Einlassöffnung ist zu klein für die gewählte Zellgröße.");
 
-  // inlet duct, closed bottom (:174-178)
+  // device: inlet duct, closed bottom, flood, leak, outlet (:174-216)
   g.kw0 = -1;
   for (int k = 0; k < nz; k++) if ((double)g.zc[k] >= g.mn[2]) { g.kw0 = k; break; }
-  uint8_t *solid = g.solid.data();
-  for (int i = 0; i < nx; i++)
-    for (int j = 0; j < ny; j++)
-      for (int k = 0; k < g.kw0; k++) solid[((int64_t)i * ny + j) * nz + k] = g.opening[(size_t)i * ny + j] ? 0 : 1;
-  for (int j = 0; j < ny; j++)
-    if ((double)g.dc[j] > g.mx[1] - 0.5 * h)
-      for (int i = 0; i < nx; i++)
-        for (int k = 0; k < nz; k++) solid[((int64_t)i * ny + j) * nz + k] = 1;
+  std::vector<uint8_t> close_row(ny, 0);
+  for (int j = 0; j < ny; j++) close_row[j] = (double)g.dc[j] > g.mx[1] - 0.5 * h ? 1 : 0;
   g.top = -1;
   for (int j = 0; j < ny; j++) if ((double)g.dc[j] >= 0) { g.top = j; break; }
   if (g.top < 0) return fail(ABX_ERR_SEAL_OUTSIDE, "Dichtebene liegt außerhalb des Modells.");
   const int top = g.top;
-  // flood from the opening, 6-connected, j >= top (:181-189)
-  g.fluid.assign((size_t)g.N, 0);
-  uint8_t *fluid = g.fluid.data();
-  std::vector<int64_t> Q;
-  Q.reserve((size_t)std::min<int64_t>(g.N, 1 << 24));
-  auto visit = [&](int64_t c, int j) {
-    if (!fluid[c] && !solid[c] && j >= top) { fluid[c] = 1; Q.push_back(c); }
-  };
-  for (int64_t c = 0; c < (int64_t)nx * ny; c++) if (g.opening[c]) visit(c * nz, (int)(c % ny));
-  for (size_t head = 0; head < Q.size(); head++) {
-    const int64_t c = Q[head];
-    const int k = (int)(c % nz);
-    const int64_t ij = c / nz;
-    const int j = (int)(ij % ny), i = (int)(ij / ny);
-    if (i > 0) visit(c - (int64_t)ny * nz, j);
-    if (i < nx - 1) visit(c + (int64_t)ny * nz, j);
-    if (j > 0) visit(c - nz, j - 1);
-    if (j < ny - 1) visit(c + nz, j + 1);
-    if (k > 0) visit(c - 1, j);
-    if (k < nz - 1) visit(c + 1, j);
+  CK(cudaMalloc((void **)&g.d_opening, std::max<size_t>(g.opening.size(), 1)), "prepare: opening");
+  CK(cudaMemcpyAsync(g.d_opening, g.opening.data(), g.opening.size(), cudaMemcpyHostToDevice, st), "prepare: opening");
+  DevBuf dclose, dflag, dcount;
+  CK(cudaMalloc(&dclose.p, ny), "prepare: rows");
+  CK(cudaMemcpyAsync(dclose.p, close_row.data(), ny, cudaMemcpyHostToDevice, st), "prepare: rows");
+  CK(cudaMalloc((void **)&g.d_fluid, (size_t)g.N), "prepare: fluid");
+  CK(cudaMalloc((void **)&g.d_outlet, (size_t)g.N), "prepare: outlet");
+  CK(cudaMalloc(&dflag.p, 2 * sizeof(int)), "prepare: flags");
+  CK(cudaMalloc(&dcount.p, 5 * sizeof(unsigned long long)), "prepare: counts");
+  MaskArgs a{nx, ny, nz, g.N, g.d_solid, g.d_fluid, g.d_outlet, g.d_opening, (const uint8_t *)dclose.p, g.kw0, top};
+  CK(prep_duct(a, st), "prepare: duct");
+  g.launches += 2;
+  g.h2d += (int64_t)(g.opening.size() + ny);
+  // flood: rounds of line sweeps until a round adds no cell (each round at least one cell otherwise)
+  int *changed = (int *)dflag.p;
+  for (int64_t round = 0;; round++) {
+    if (round > g.N) return fail(ABX_ERR_CUDA, "prepare: flood fill did not settle");
+    CK(cudaMemsetAsync(changed, 0, sizeof(int), st), "prepare: flood");
+    CK(prep_flood_round(a, changed, st), "prepare: flood");
+    int c = 0;
+    CK(cudaMemcpyAsync(&c, changed, sizeof(int), cudaMemcpyDeviceToHost, st), "prepare: flood");
+    CK(cudaStreamSynchronize(st), "prepare: flood");
+    g.launches += 3;
+    g.d2h += sizeof(int);
+    if (!c) break;
   }
-  int64_t qtot = (int64_t)Q.size();
   // leak: fluid on the side faces or the far face (:191-195)
-  bool leaked = false;
-  for (int i = 0; i < nx && !leaked; i++)
-    for (int j = top; j < ny && !leaked; j++)
-      for (int k = g.kw0; k < nz; k++)
-        if ((i == 0 || i == nx - 1 || k == nz - 1) && fluid[((int64_t)i * ny + j) * nz + k]) { leaked = true; break; }
+  int *leak = (int *)dflag.p + 1;
+  CK(cudaMemsetAsync(leak, 0, sizeof(int), st), "prepare: leak");
+  CK(prep_leak(a, leak, st), "prepare: leak");
+  int leaked = 0;
+  CK(cudaMemcpyAsync(&leaked, leak, sizeof(int), cudaMemcpyDeviceToHost, st), "prepare: leak");
+  CK(cudaStreamSynchronize(st), "prepare: leak");
+  g.launches += 1;
+  g.d2h += sizeof(int);
   if (leaked) {
     char hs[40];
     fmt_number(hs, sizeof hs, h);
@@ -310,41 +315,38 @@ static int finish_geometry(abx_geom &g, const abx_prepare_params *p, const std::
                 hs);
   }
   // outlet: lid plenum with a round outlet, or the whole row `top` (:197-213)
-  g.outlet.assign((size_t)g.N, 0);
-  g.nOut = 0;
+  unsigned long long *cnt = (unsigned long long *)dcount.p;
+  CK(cudaMemsetAsync(cnt, 0, 5 * sizeof(unsigned long long), st), "prepare: outlet");
+  int jpt = -1;
+  double L[3] = {0, 0, 0}, r2 = 0;
   if (g.has_outlet) {
     g.jpt = first_ge(g.dc, -p->outlet_height);
     if (g.jpt >= top) return fail(ABX_ERR_LID_TOO_LOW, "Deckelhöhe ist kleiner als eine Zelle.");
-    double L[3];
+    jpt = g.jpt;
     g.fr.local(p->outlet_center, L);
-    const double r2 = (p->outlet_diameter / 2) * (p->outlet_diameter / 2);
-    for (int i = 0; i < nx; i++)
-      for (int k = 0; k < nz; k++) {
-        if (!fluid[((int64_t)i * ny + top) * nz + k]) continue;
-        for (int j = g.jpt; j < top; j++) {
-          const int64_t c = ((int64_t)i * ny + j) * nz + k;
-          fluid[c] = 1; solid[c] = 0; qtot++;
-        }
-        const double ddx = (double)g.xc[i] - L[0], ddz = (double)g.zc[k] - L[2];
-        if (ddx * ddx + ddz * ddz <= r2) { g.outlet[((int64_t)i * ny + g.jpt) * nz + k] = 1; g.nOut++; }
-      }
-    if (g.nOut < 4) return fail(ABX_ERR_BAD_OUTLET, "Der Auslass liegt nicht über der Filterfläche oder ist zu klein.");
-  } else {
-    for (int i = 0; i < nx; i++)
-      for (int k = 0; k < nz; k++) {
-        const int64_t c = ((int64_t)i * ny + top) * nz + k;
-        if (fluid[c]) { g.outlet[c] = 1; g.nOut++; }
-      }
+    r2 = (p->outlet_diameter / 2) * (p->outlet_diameter / 2);
   }
-  g.nf = (int)qtot;
+  DevBuf dxc, dzc;
+  CK(cudaMalloc(&dxc.p, sizeof(float) * nx), "prepare: outlet");
+  CK(cudaMalloc(&dzc.p, sizeof(float) * nz), "prepare: outlet");
+  CK(cudaMemcpyAsync(dxc.p, g.xc.data(), sizeof(float) * nx, cudaMemcpyHostToDevice, st), "prepare: outlet");
+  CK(cudaMemcpyAsync(dzc.p, g.zc.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st), "prepare: outlet");
+  CK(prep_outlet(a, jpt, (const float *)dxc.p, (const float *)dzc.p, L[0], L[2], r2, cnt, st), "prepare: outlet");
+  // counts after the plenum (:214-216): cells, filter-layer cells, cells on the outlet row
   g.jm = first_ge(g.dc, g.pleat / 2);
-  g.Af = 0;
-  g.leak = 0;
-  for (int i = 0; i < nx; i++)
-    for (int k = 0; k < nz; k++) {
-      g.Af += fluid[((int64_t)i * ny + g.jm) * nz + k];
-      g.leak += fluid[((int64_t)i * ny + top) * nz + k];
-    }
+  CK(prep_counts(a, g.jm, cnt + 2, st), "prepare: counts");
+  unsigned long long hc[5];
+  CK(cudaMemcpyAsync(hc, cnt, sizeof hc, cudaMemcpyDeviceToHost, st), "prepare: counts");
+  CK(cudaStreamSynchronize(st), "prepare: counts");
+  g.launches += 2;
+  g.h2d += (int64_t)(sizeof(float) * (nx + nz));
+  g.d2h += sizeof hc;
+  g.nOut = (int)hc[1];
+  if (g.has_outlet && g.nOut < 4)
+    return fail(ABX_ERR_BAD_OUTLET, "Der Auslass liegt nicht über der Filterfläche oder ist zu klein.");
+  g.nf = (int)hc[2];
+  g.Af = (int)hc[3];
+  g.leak = (int)hc[4];
   return ABX_OK;
 }
 
@@ -359,98 +361,85 @@ static uint2 seg2(uint32_t base, uint32_t lanes) {
 
 // The k offset in [0,32) that packs the columns' fluid cells into the fewest
 // 32-cell segments (whole warps of fluid cells in the step kernels).
-static int64_t choose_kpad(const abx_geom &g) {
-  std::vector<int64_t> count(32, 0);
-  const int nz = g.nz;
-  for (int64_t ij = 0; ij < (int64_t)g.nx * g.ny; ij++) {
-    const uint8_t *col = g.fluid.data() + ij * nz;
-    int k = 0;
-    int64_t last[32];
-    for (int t = 0; t < 32; t++) last[t] = -1;
-    while (k < nz) {
-      while (k < nz && !col[k]) k++;
-      if (k >= nz) break;
-      const int a = k;
-      while (k < nz && col[k]) k++;
-      const int b = k - 1;  // fluid run [a, b]
-      for (int t = 0; t < 32; t++) {
-        int64_t s0 = (a + t) / 32, s1 = (b + t) / 32;
-        if (s0 == last[t]) s0++;
-        if (s1 >= s0) count[t] += s1 - s0 + 1;
-        last[t] = s1;
-      }
-    }
-  }
-  int64_t best = 0;
-  for (int t = 1; t < 32; t++) if (count[t] < count[best]) best = t;
-  return best;
-}
-
 static int build_device_geometry(abx_geom &g, cudaStream_t st) {
   const int nx = g.nx, ny = g.ny, nz = g.nz;
-  g.kpad = choose_kpad(g);
+  MaskArgs a{nx, ny, nz, g.N, g.d_solid, g.d_fluid, g.d_outlet, g.d_opening, nullptr, g.kw0, g.top};
+  // kpad: the column shift with the fewest 32-cell runs holding air (first of equals)
+  const int W = (nz + 31) / 32 + 1;
+  DevBuf dbits, dkc;
+  CK(cudaMalloc(&dbits.p, sizeof(uint32_t) * (size_t)nx * ny * W), "prepare: column bits");
+  CK(cudaMalloc(&dkc.p, 32 * sizeof(unsigned long long)), "prepare: kpad");
+  CK(cudaMemsetAsync(dkc.p, 0, 32 * sizeof(unsigned long long), st), "prepare: kpad");
+  CK(prep_kpad_counts(a, W, (uint32_t *)dbits.p, (unsigned long long *)dkc.p, st), "prepare: kpad");
+  unsigned long long kc[32];
+  CK(cudaMemcpyAsync(kc, dkc.p, sizeof kc, cudaMemcpyDeviceToHost, st), "prepare: kpad");
+  CK(cudaStreamSynchronize(st), "prepare: kpad");
+  int best = 0;
+  for (int t = 1; t < 32; t++) if (kc[t] < kc[best]) best = t;
+  g.kpad = best;
   g.nzp = (g.nz + g.kpad + 31) / 32 * 32;
   g.Np = (int64_t)g.nx * g.ny * g.nzp;
   if (19 * g.Np >= (1ll << 32)) return fail(ABX_ERR_INVALID_ARGUMENT, "prepare: grid above 2^32 / 19 padded cells");
+  // classes (setupSim :248-255) and the cell mask words
   const double dtop = g.dc[g.top];
-  g.cls.assign((size_t)g.N, 0);
-  g.cells_p.clear();
-  g.cells_j.clear();
-  g.cells_p.reserve(g.nf);
-  g.cells_j.reserve(g.nf);
-  g.Ain = 0;
+  std::vector<uint8_t> filt(ny, 0);
   g.Lp = 0;
-  for (int j = 0; j < ny; j++) if ((double)g.dc[j] > dtop && (double)g.dc[j] <= g.pleat) g.Lp++;
-  for (int i = 0; i < nx; i++)
-    for (int j = 0; j < ny; j++) {
-      const bool filt = (double)g.dc[j] > dtop && (double)g.dc[j] <= g.pleat;
-      for (int k = 0; k < nz; k++) {
-        const int64_t c = ((int64_t)i * ny + j) * nz + k;
-        if (!g.fluid[c]) continue;
-        uint8_t cl = 1;
-        if (k == 0 && g.opening[(size_t)i * ny + j]) { cl = 2; g.Ain++; }
-        else if (g.outlet[c]) cl = 3;
-        else if (filt) cl = 4;
-        g.cls[c] = cl;
-        g.cells_p.push_back(((int64_t)i * ny + j) * g.nzp + k + g.kpad);
-        g.cells_j.push_back(j);
-      }
-    }
-  // fluid segments: 32-cell runs along k holding any fluid cell, with the lane mask of their fluid cells
-  std::vector<uint2> seg;
-  for (int64_t ij = 0; ij < (int64_t)nx * ny; ij++) {
-    int64_t cur = -1;
-    uint32_t lanes = 0;
-    for (int k = 0; k < nz; k++) {
-      if (!g.cls[ij * nz + k]) continue;
-      const int64_t kk = k + g.kpad, s0 = kk / 32;
-      if (s0 != cur) {
-        if (cur >= 0) seg.push_back(seg2((uint32_t)(ij * g.nzp + cur * 32), lanes));
-        cur = s0;
-        lanes = 0;
-      }
-      lanes |= 1u << (kk % 32);
-    }
-    if (cur >= 0) seg.push_back(seg2((uint32_t)(ij * g.nzp + cur * 32), lanes));
-  }
-  g.nseg = (uint32_t)seg.size();
-  DevBuf dcls;
+  for (int j = 0; j < ny; j++)
+    if ((double)g.dc[j] > dtop && (double)g.dc[j] <= g.pleat) { filt[j] = 1; g.Lp++; }
+  DevBuf dfilt, dcls, dain;
+  CK(cudaMalloc(&dfilt.p, ny), "prepare: classes");
+  CK(cudaMemcpyAsync(dfilt.p, filt.data(), ny, cudaMemcpyHostToDevice, st), "prepare: classes");
   CK(cudaMalloc(&dcls.p, (size_t)g.N), "prepare: class array");
-  CK(cudaMemcpyAsync(dcls.p, g.cls.data(), (size_t)g.N, cudaMemcpyHostToDevice, st), "prepare: class upload");
-  g.h2d += g.N + (int64_t)(sizeof(uint2) * seg.size() + g.opening.size() + sizeof(int64_t) * g.cells_p.size());
-  g.launches += 1;
+  CK(cudaMalloc(&dain.p, sizeof(unsigned long long)), "prepare: classes");
+  CK(cudaMemsetAsync(dain.p, 0, sizeof(unsigned long long), st), "prepare: classes");
+  CK(prep_classes(a, (const uint8_t *)dfilt.p, (uint8_t *)dcls.p, (unsigned long long *)dain.p, st), "prepare: classes");
   CK(cudaMalloc((void **)&g.d_mask, sizeof(uint32_t) * (size_t)g.Np), "prepare: mask");
   CK(launch_build_mask((const uint8_t *)dcls.p, nx, ny, nz, g.nzp, g.kpad, g.d_mask, st), "prepare: build mask");
-  CK(cudaMalloc((void **)&g.d_seg, sizeof(uint2) * std::max<size_t>(seg.size(), 1)), "prepare: segments");
-  if (!seg.empty())
-    CK(cudaMemcpyAsync(g.d_seg, seg.data(), sizeof(uint2) * seg.size(), cudaMemcpyHostToDevice, st), "prepare: segments");
-  CK(cudaMalloc((void **)&g.d_opening, std::max<size_t>(g.opening.size(), 1)), "prepare: opening");
-  CK(cudaMemcpyAsync(g.d_opening, g.opening.data(), g.opening.size(), cudaMemcpyHostToDevice, st), "prepare: opening");
-  CK(cudaMalloc((void **)&g.d_cells, sizeof(int64_t) * std::max<size_t>(g.cells_p.size(), 1)), "prepare: cells");
-  if (!g.cells_p.empty())
-    CK(cudaMemcpyAsync(g.d_cells, g.cells_p.data(), sizeof(int64_t) * g.cells_p.size(), cudaMemcpyHostToDevice, st),
-       "prepare: cells");
-  CK(cudaStreamSynchronize(st), "prepare: sync");
+  // compact cell list, in (i, j, k) order
+  const int64_t nb = prep_compact_blocks(g.N);
+  DevBuf dbc, doff;
+  CK(cudaMalloc(&dbc.p, sizeof(uint32_t) * std::max<int64_t>(nb, 1)), "prepare: compaction");
+  CK(cudaMalloc(&doff.p, sizeof(unsigned long long) * (nb + 1)), "prepare: compaction");
+  CK(cudaMalloc((void **)&g.d_cells, sizeof(int64_t) * std::max(g.nf, 1)), "prepare: cells");
+  CK(prep_cells(a, g.nzp, g.kpad, g.d_cells, (uint32_t *)dbc.p, (unsigned long long *)doff.p, st), "prepare: cells");
+  unsigned long long ncells = 0;
+  CK(cudaMemcpyAsync(&ncells, (unsigned long long *)doff.p + nb, sizeof ncells, cudaMemcpyDeviceToHost, st), "prepare: cells");
+  // fluid segments: 32-cell runs along k holding air, with their lane masks
+  const int64_t S = g.nzp / 32, nslot = (int64_t)nx * ny * S, nb2 = prep_compact_blocks(nslot);
+  DevBuf dbc2, doff2;
+  CK(cudaMalloc(&dbc2.p, sizeof(uint32_t) * std::max<int64_t>(nb2, 1)), "prepare: segments");
+  CK(cudaMalloc(&doff2.p, sizeof(unsigned long long) * (nb2 + 1)), "prepare: segments");
+  CK(prep_segments(a, W, (const uint32_t *)dbits.p, g.nzp, g.kpad, nullptr, (uint32_t *)dbc2.p,
+                   (unsigned long long *)doff2.p, st), "prepare: segments");
+  unsigned long long nseg = 0, ain = 0;
+  CK(cudaMemcpyAsync(&nseg, (unsigned long long *)doff2.p + nb2, sizeof nseg, cudaMemcpyDeviceToHost, st), "prepare: segments");
+  CK(cudaMemcpyAsync(&ain, dain.p, sizeof ain, cudaMemcpyDeviceToHost, st), "prepare: classes");
+  CK(cudaStreamSynchronize(st), "prepare: segments");
+  if ((int64_t)ncells != g.nf) return fail(ABX_ERR_CUDA, "prepare: cell list has %llu cells, expected %d", ncells, g.nf);
+  g.Ain = (int)ain;
+  g.nseg = (uint32_t)nseg;
+  CK(cudaMalloc((void **)&g.d_seg, sizeof(uint2) * std::max<unsigned long long>(nseg, 1)), "prepare: segments");
+  CK(prep_segments(a, W, (const uint32_t *)dbits.p, g.nzp, g.kpad, g.d_seg, (uint32_t *)dbc2.p,
+                   (unsigned long long *)doff2.p, st), "prepare: segments");
+  // the air of layers jm and top+1 in compact order (the progress probe's cells, :327-333)
+  auto layer = [&](int j, std::vector<int64_t> &out) -> int {
+    out.clear();
+    if (j < 0 || j >= ny) return ABX_OK;
+    std::vector<uint8_t> lay((size_t)nx * nz);
+    CK(cudaMemcpy2DAsync(lay.data(), nz, g.d_fluid + (size_t)j * nz, (size_t)ny * nz, nz, nx, cudaMemcpyDeviceToHost, st),
+       "prepare: layers");
+    CK(cudaStreamSynchronize(st), "prepare: layers");
+    g.d2h += (int64_t)lay.size();
+    for (int i = 0; i < nx; i++)
+      for (int k = 0; k < nz; k++)
+        if (lay[(size_t)i * nz + k]) out.push_back(((int64_t)i * ny + j) * g.nzp + k + g.kpad);
+    return ABX_OK;
+  };
+  if (int rc = layer(g.jm, g.layer_m)) return rc;
+  if (int rc = layer(g.top + 1, g.layer_t)) return rc;
+  g.launches += 9;
+  g.h2d += ny;
+  g.d2h += (int64_t)(sizeof kc + 3 * sizeof(unsigned long long));
   return ABX_OK;
 }
 
@@ -517,6 +506,8 @@ extern "C" int abx_prepare(const float *tris, size_t nfloats, const abx_prepare_
   for (int k = 0; k < g.nz; k++) g.zc[k] = (float)(g.origin[2] + (k + 0.5) * h);
 
   // GPU: voxelize at 3x oversampling and downsample (:125-135)
+  using clk = std::chrono::steady_clock;
+  const auto t0 = clk::now();
   CK(cudaSetDevice(g.device), "prepare: set device");
   StreamHolder sh;
   CK(cudaStreamCreateWithFlags(&sh.s, cudaStreamNonBlocking), "prepare: stream");
@@ -530,18 +521,24 @@ extern "C" int abx_prepare(const float *tris, size_t nfloats, const abx_prepare_
   VoxJob job{(const float *)dtris.p, ntri, {g.origin[0], g.origin[1], g.origin[2]}, hf, g.nx, g.ny, g.nz, g.kf};
   VoxOut vo{(uint8_t *)dsolid.p, (uint8_t *)dslice.p, nullptr};
   CK(run_voxelizer(job, vo, sh.s), "prepare: voxelize");
-  g.solid.resize((size_t)g.N);
   std::vector<uint8_t> slice((size_t)g.nxf * g.nyf);
-  CK(cudaMemcpyAsync(g.solid.data(), dsolid.p, (size_t)g.N, cudaMemcpyDeviceToHost, sh.s), "prepare: download");
   CK(cudaMemcpyAsync(slice.data(), dslice.p, slice.size(), cudaMemcpyDeviceToHost, sh.s), "prepare: download");
   CK(cudaStreamSynchronize(sh.s), "prepare: sync");
+  g.d_solid = (uint8_t *)dsolid.p;   // the geometry keeps the solid mask on the device
+  dsolid.p = nullptr;
   g.launches += vo.launches;
   g.h2d += (int64_t)(sizeof(float) * nfloats);
-  g.d2h += vo.d2h_bytes + g.N + (int64_t)slice.size();
-  int rc = finish_geometry(g, p, slice);
+  g.d2h += vo.d2h_bytes + (int64_t)slice.size();
+  const auto t1 = clk::now();
+  int rc = finish_geometry(g, p, slice, sh.s);
   if (rc) return rc;
+  const auto t2 = clk::now();
   rc = build_device_geometry(g, sh.s);
   if (rc) return rc;
+  const auto t3 = clk::now();
+  g.ms_vox = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  g.ms_masks = std::chrono::duration<double, std::milli>(t2 - t1).count();
+  g.ms_device = std::chrono::duration<double, std::milli>(t3 - t2).count();
   *out = G.release();
   return ABX_OK;
 }
@@ -565,16 +562,19 @@ extern "C" int abx_geom_get_info(const abx_geom *g, abx_geom_info *o) {
   o->outlet_cm2_real = g->has_outlet ? g->nOut * h * h / 100 : 0;
   o->frame_cy = g->fr.cy; o->frame_sy = g->fr.sy;
   o->kernel_launches = g->launches; o->h2d_bytes = g->h2d; o->d2h_bytes = g->d2h;
+  o->ms_voxelize = g->ms_vox; o->ms_masks = g->ms_masks; o->ms_device = g->ms_device;
   return ABX_OK;
 }
 
 extern "C" int abx_geom_get_masks(const abx_geom *g, uint8_t *solid, uint8_t *fluid, uint8_t *opening,
                                   uint8_t *outlet, float *xc, float *dc, float *zc) {
+  clear_stale_error();
   if (!g) return fail(ABX_ERR_INVALID_ARGUMENT, "geom_get_masks: null geometry");
-  if (solid) std::memcpy(solid, g->solid.data(), g->solid.size());
-  if (fluid) std::memcpy(fluid, g->fluid.data(), g->fluid.size());
+  if (solid || fluid || outlet) CK(cudaSetDevice(g->device), "geom_get_masks");
+  if (solid) CK(cudaMemcpy(solid, g->d_solid, (size_t)g->N, cudaMemcpyDeviceToHost), "geom_get_masks");
+  if (fluid) CK(cudaMemcpy(fluid, g->d_fluid, (size_t)g->N, cudaMemcpyDeviceToHost), "geom_get_masks");
+  if (outlet) CK(cudaMemcpy(outlet, g->d_outlet, (size_t)g->N, cudaMemcpyDeviceToHost), "geom_get_masks");
   if (opening) std::memcpy(opening, g->opening.data(), g->opening.size());
-  if (outlet) std::memcpy(outlet, g->outlet.data(), g->outlet.size());
   if (xc) std::memcpy(xc, g->xc.data(), sizeof(float) * g->xc.size());
   if (dc) std::memcpy(dc, g->dc.data(), sizeof(float) * g->dc.size());
   if (zc) std::memcpy(zc, g->zc.data(), sizeof(float) * g->zc.size());
@@ -709,10 +709,9 @@ extern "C" int abx_sim_create(abx_geom *g, const abx_run_params *p, const float 
   s.g = g; s.p = *p; s.device = g->device;
   // setupSim scalars (src/engine.js:246-263)
   s.Ain = g->Ain; s.Lp = g->Lp;
-  std::vector<int64_t> plist;
-  for (int a = 0; a < g->nf; a++) if (g->cells_j[a] == g->jm) plist.push_back(g->cells_p[a]);
+  std::vector<int64_t> plist(g->layer_m);
   s.nM = (int)plist.size();
-  for (int a = 0; a < g->nf; a++) if (g->cells_j[a] == g->top + 1) plist.push_back(g->cells_p[a]);
+  plist.insert(plist.end(), g->layer_t.begin(), g->layer_t.end());
   s.nT = (int)plist.size() - s.nM;
   s.Af = s.nM;
   s.u0 = p->u; s.tau0 = p->tau; s.aniso = p->aniso;

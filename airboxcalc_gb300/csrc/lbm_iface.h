@@ -134,6 +134,40 @@ cudaError_t run_voxelizer(const VoxJob &job, VoxOut &out, cudaStream_t st);
 int voxelize_static(const float *d_tris, size_t nfloats, const double origin[3], double h, int nx, int ny, int nz,
                     uint8_t *d_vox, cudaStream_t st, char *msg, size_t msg_len);
 
+// ---------------------------------------------------------------- prepare stages (prepare.cu)
+struct MaskArgs {
+  int nx, ny, nz;
+  int64_t N;
+  uint8_t *solid, *fluid, *outlet;   // N bytes each, index (i*ny + j)*nz + k
+  const uint8_t *opening;            // nx*ny
+  const uint8_t *close_row;          // ny: rows made solid (beyond the model's depth)
+  int kw0, top;
+};
+// duct and closing rows into solid, fluid/outlet cleared, the opening's k = 0 cells seeded
+cudaError_t prep_duct(const MaskArgs &a, cudaStream_t st);
+// one round of line sweeps along k, j, i; *changed |= 1 when a cell joined the air
+cudaError_t prep_flood_round(const MaskArgs &a, int *changed, cudaStream_t st);
+cudaError_t prep_leak(const MaskArgs &a, int *leak, cudaStream_t st);
+// jpt >= 0: lid plenum from row jpt (counts[0] += cells added) with a round outlet of radius^2 r2 around
+// (cx, cz) at row jpt; jpt < 0: row `top` is the outlet.  counts[1] += outlet cells
+cudaError_t prep_outlet(const MaskArgs &a, int jpt, const float *xc, const float *zc, double cx, double cz, double r2,
+                        unsigned long long *counts, cudaStream_t st);
+// counts[0..2] += air cells, air on layer jm, air on row top
+cudaError_t prep_counts(const MaskArgs &a, int jm, unsigned long long *counts, cudaStream_t st);
+// setupSim classes (0 no air, 1 bulk, 2 inlet, 3 outlet, 4 filter) into cls; *ain += inlet cells
+cudaError_t prep_classes(const MaskArgs &a, const uint8_t *filt_row, uint8_t *cls, unsigned long long *ain,
+                         cudaStream_t st);
+// air bits per column (W words each) into bits; count[t] += 32-cell runs holding air at column shift t
+cudaError_t prep_kpad_counts(const MaskArgs &a, int W, uint32_t *bits, unsigned long long *count, cudaStream_t st);
+// ordered compactions: the padded index of every air cell, and the {base, lanes} of every 32-cell run
+// holding air (out may be null: offsets[blocks] then receives the count only); block_counts and offsets
+// hold prep_compact_blocks(items) and prep_compact_blocks(items) + 1 entries
+int64_t prep_compact_blocks(int64_t n);
+cudaError_t prep_cells(const MaskArgs &a, int64_t nzp, int64_t kpad, int64_t *cells, uint32_t *block_counts,
+                       unsigned long long *offsets, cudaStream_t st);
+cudaError_t prep_segments(const MaskArgs &a, int W, const uint32_t *bits, int64_t nzp, int64_t kpad, uint2 *seg,
+                          uint32_t *block_counts, unsigned long long *offsets, cudaStream_t st);
+
 // ---------------------------------------------------------------- post-processing (postproc.cu)
 struct PostArgs {
   int nx, ny, nz;

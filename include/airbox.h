@@ -102,6 +102,8 @@ typedef struct {
   double frame_cy, frame_sy;  /* cos/sin of the yaw used by the frame */
   int64_t kernel_launches;    /* kernels prepare() launched */
   int64_t h2d_bytes, d2h_bytes;  /* bytes prepare() copied host->device / device->host */
+  double ms_voxelize, ms_masks, ms_device;  /* wall time: GPU voxelizer (incl. read-back), opening/duct/flood/
+                                               leak/outlet, classes/segments/device arrays */
 } abx_geom_info;
 int abx_geom_get_info(const abx_geom *g, abx_geom_info *out);
 /* Host copies of g.solid / g.fluid / g.outlet (N bytes each, index (i*ny+j)*nz+k),
