@@ -82,3 +82,18 @@ def test_warm_start_and_batch_entry_points_check_arguments_without_gpu():
     assert L.abx_sim_converge(None, None, C.byref(r)) == A.ERR_INVALID_ARGUMENT
     assert L.abx_batch_create(None, None, 0, C.byref(h)) == A.ERR_INVALID_ARGUMENT
     assert L.abx_sim_streamlines(None, 220, None, None, None, 0, 0, None) == A.ERR_INVALID_ARGUMENT
+
+
+def test_prepare_rejects_grids_beyond_32_bit_offsets_before_any_gpu_work():
+    """The step kernels index populations with 32-bit offsets: 19 * padded cells must stay below 2^32."""
+    from airboxcalc_gb300 import engine as E
+    tris = np.array([[0, 0, 0], [3000, 0, 0], [0, 3000, 0], [0, 0, 0], [0, 0, 3000], [3000, 0, 0]],
+                    np.float32).ravel()
+    p = {"tris": tris, "dx": 1.0, "sealAxis": 1, "sealSign": -1, "seal": 0, "inletAxis": 2, "inletSign": -1,
+         "inletYaw": 0, "pleat": 40, "maxCells": 1e12}
+    with pytest.raises(E.AirboxError) as ei:
+        E.prepare(p)
+    assert ei.value.code == A.ERR_INVALID_ARGUMENT and "2^32" in str(ei.value)
+    with pytest.raises(E.AirboxError) as ei:
+        E.prepare({**p, "maxCells": 4.5e6})               # the reference's own cap comes first
+    assert ei.value.code == A.ERR_GRID_TOO_LARGE and "Gitter zu groß" in str(ei.value)
