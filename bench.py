@@ -207,9 +207,9 @@ def solve(g, run, storage, timing=True):
     return res["metrics"], S.get_acc(), t["run_ms"] + t["eval_ms"], S.NF
 
 
-def study_precision(spec, run, desc):
+def study_precision(spec, run, desc, storages=("f64", "f32exact", "f32", "f16", "bf16")):
     """KPI and field error of every population storage against the float64 run
-    (same airbox, same steps)."""
+    (same airbox, same steps), with each run's MLUPS and the GB/s of its population bytes."""
     import numpy as np
     from airboxcalc_gb300 import engine as E
     g = E.prepare({"tris": __import__("airboxcalc_gb300.airboxgen", fromlist=["x"]).build_airbox(spec),
@@ -217,7 +217,8 @@ def study_precision(spec, run, desc):
     ref_m, ref_acc, ref_ms, NF = solve(g, run, "f64")
     ra = ref_acc.reshape(4, -1).astype(np.float64)
     rows = []
-    for st in ("f64", "f32exact", "f32", "f16", "bf16"):
+    bytes_per_update = {"f64": 304, "f32exact": 152, "f32": 152, "f16": 76, "bf16": 76}
+    for st in storages:
         m, acc, ms, _ = (ref_m, ref_acc, ref_ms, NF) if st == "f64" else solve(g, run, st)
         a = acc.reshape(4, -1).astype(np.float64)
         err = {k: (m[k] - ref_m[k]) / abs(ref_m[k]) if ref_m[k] else m[k] - ref_m[k] for k in KPI}
@@ -225,6 +226,7 @@ def study_precision(spec, run, desc):
         l2r = float(np.linalg.norm(a[3] - ra[3]) / np.linalg.norm(ra[3] - 1.0))
         rows.append({"study": "precision", "workload": desc, "storage": st, "NF": NF,
                      "steps": run["steps"], "ms": round(ms, 2), "mlups": round(NF * run["steps"] / ms / 1e3, 1),
+                     "population_GBs": round(bytes_per_update[st] * NF * run["steps"] / ms / 1e6, 1),
                      "kpi": {k: round(m[k], 6) for k in KPI}, "rel_err_vs_f64": {k: float(f"{v:.3e}") for k, v in err.items()},
                      "rel_l2_u_vs_f64": float(f"{l2u:.3e}"), "rel_l2_rho_minus_1_vs_f64": float(f"{l2r:.3e}")})
         print(json.dumps(rows[-1]), flush=True)
@@ -453,12 +455,13 @@ def main():
                     help="instead of the bench line: KPI error per storage vs float64, steps/time to converged "
                          "KPIs, or the learned warm start on held-out airboxes")
     ap.add_argument("--seeds", default="6000:6200", help="held-out seed range a:b of --study warmstart")
+    ap.add_argument("--storages", default="f64,f32exact,f32,f16,bf16", help="storages of --study precision")
     ap.add_argument("--weights", default=None, help="warm-start network weights (.npz)")
     a = ap.parse_args()
     ws, rank, local = dist_env()
     spec, run, desc = workload(a.workload)
     if a.study == "precision":
-        study_precision(spec, run, desc)
+        study_precision(spec, run, desc, tuple(a.storages.split(",")))
         return 0
     if a.study == "converge":
         study_converge(spec, run, desc)
