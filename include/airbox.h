@@ -273,7 +273,7 @@ int abx_voxelize_static(const float *d_tris, size_t nfloats, const double origin
  * The network is a 3-D convolutional encoder-decoder on an R^3 resampling
  * of the grid (levels L, channels base << l).  Input: fluid / inlet /
  * outlet / filter fraction of each voxel's footprint, wall distance, K and
- * the grid extent; output: the time-averaged u / u0 and (rho - 1)/(15 u0^2).
+ * the grid extent; output: the time-averaged u / u0 and (rho - 1)/(5 u0^2).
  * Training, inference, the resampling and the equilibrium initialisation
  * all run in the library's CUDA kernels on the network's device.
  * ====================================================================== */
