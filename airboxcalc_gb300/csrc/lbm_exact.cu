@@ -12,7 +12,7 @@ namespace abx {
 template <int K>
 static cudaError_t step_k(bool odd, bool acc, bool has_ns, const StepArgs &a, cudaStream_t st) {
   if (a.nseg == 0) return cudaSuccess;
-  const dim3 grid((a.nseg + 8 * kStepSpw - 1) / (8 * kStepSpw)), block(256);
+  const dim3 grid(step_grid(a.nseg)), block(256);
 #define ABX_L(O, A, N) aa_step_kernel<K, O, A, N><<<grid, block, 0, st>>>(a)
   if (odd) {
     if (acc) { if (has_ns) ABX_L(true, true, true); else ABX_L(true, true, false); }
