@@ -44,9 +44,13 @@ template <int K> struct Store;
 #define ABX_CACHE_HINTS 1
 #endif
 // ld/st address global memory; lds reads a value staged in shared memory.
+// Every format also has raw accessors (ldr / ldsr / str) that the step kernels use: the stored value itself,
+// i.e. f for the plain formats and h = f - w_q for the shifted ones (whose collision then works on h).
 template <> struct Store<kStoreF32> {
   using T = float; using L = float; using Acc = float;
+  static constexpr bool kShifted = false;
   __device__ static __forceinline__ L lds(const T *p, L) { return *p; }
+  __device__ static __forceinline__ L ldsr(const T *p) { return *p; }
 #if ABX_CACHE_HINTS == 2
   __device__ static __forceinline__ L ld(const T *p, L) { return __ldcs(p); }
 #else
@@ -57,30 +61,48 @@ template <> struct Store<kStoreF32> {
 #else
   __device__ static __forceinline__ void st(T *p, L v, L) { *p = v; }
 #endif
+  __device__ static __forceinline__ L ldr(const T *p) { return ld(p, 0.0f); }
+  __device__ static __forceinline__ void str(T *p, L v) { st(p, v, 0.0f); }
 };
 template <> struct Store<kStoreF32Exact> {
   using T = float; using L = double; using Acc = float;
+  static constexpr bool kShifted = false;
   __device__ static __forceinline__ L lds(const T *p, L) { return (L)*p; }
   __device__ static __forceinline__ L ld(const T *p, L) { return (L)*p; }
   __device__ static __forceinline__ void st(T *p, L v, L) { *p = (float)v; }
+  __device__ static __forceinline__ L ldsr(const T *p) { return (L)*p; }
+  __device__ static __forceinline__ L ldr(const T *p) { return (L)*p; }
+  __device__ static __forceinline__ void str(T *p, L v) { *p = (float)v; }
 };
 template <> struct Store<kStoreF16> {
   using T = __half; using L = float; using Acc = float;
+  static constexpr bool kShifted = true;
   __device__ static __forceinline__ L lds(const T *p, L w) { return w + __half2float(*p); }
   __device__ static __forceinline__ L ld(const T *p, L w) { return w + __half2float(*p); }
   __device__ static __forceinline__ void st(T *p, L v, L w) { *p = __float2half_rn(v - w); }
+  __device__ static __forceinline__ L ldsr(const T *p) { return __half2float(*p); }
+  __device__ static __forceinline__ L ldr(const T *p) { return __half2float(*p); }
+  __device__ static __forceinline__ void str(T *p, L h) { *p = __float2half_rn(h); }
 };
 template <> struct Store<kStoreBF16> {
   using T = __nv_bfloat16; using L = float; using Acc = float;
+  static constexpr bool kShifted = true;
   __device__ static __forceinline__ L lds(const T *p, L w) { return w + __bfloat162float(*p); }
   __device__ static __forceinline__ L ld(const T *p, L w) { return w + __bfloat162float(*p); }
   __device__ static __forceinline__ void st(T *p, L v, L w) { *p = __float2bfloat16_rn(v - w); }
+  __device__ static __forceinline__ L ldsr(const T *p) { return __bfloat162float(*p); }
+  __device__ static __forceinline__ L ldr(const T *p) { return __bfloat162float(*p); }
+  __device__ static __forceinline__ void str(T *p, L h) { *p = __float2bfloat16_rn(h); }
 };
 template <> struct Store<kStoreF64> {
   using T = double; using L = double; using Acc = double;
+  static constexpr bool kShifted = false;
   __device__ static __forceinline__ L lds(const T *p, L) { return *p; }
   __device__ static __forceinline__ L ld(const T *p, L) { return *p; }
   __device__ static __forceinline__ void st(T *p, L v, L) { *p = v; }
+  __device__ static __forceinline__ L ldsr(const T *p) { return *p; }
+  __device__ static __forceinline__ L ldr(const T *p) { return *p; }
+  __device__ static __forceinline__ void str(T *p, L v) { *p = v; }
 };
 
 template <class L> __device__ __forceinline__ L weight(int q) {
@@ -192,7 +214,7 @@ __device__ __forceinline__ void collide(const L (&fi)[19], uint32_t cls, L nsv, 
 // exactly rho/3 I + rho u u on D3Q19), and equilibrium plus BGK per opposite
 // pair from a shared even part and an odd part.  Same model as collide();
 // about a third of its arithmetic.
-template <bool HAS_NS>
+template <bool HAS_NS, bool SHIFTED = false>
 __device__ __forceinline__ void collide_fast(const float (&f)[19], uint32_t cls, float nsv_in,
                                              const CollideParams<float> &P, float (&fo)[19], float &ux, float &uy,
                                              float &uz, float &rho) {
@@ -210,7 +232,10 @@ __device__ __forceinline__ void collide_fast(const float (&f)[19], uint32_t cls,
   const float s15 = f[15] + f[16], d15 = f[15] - f[16];
   const float s17 = f[17] + f[18], d17 = f[17] - f[18];
   const float sxy = s7 + s9, sxz = s11 + s13, syz = s15 + s17;
-  rho = f[0] + ((s1 + s3) + s5) + ((sxy + sxz) + syz);
+  // SHIFTED: f holds h = f - w_q; the weights add 1 to the density and 1/3 to each diagonal stress sum and
+  // cancel from every odd moment
+  const float tot = f[0] + ((s1 + s3) + s5) + ((sxy + sxz) + syz);
+  rho = SHIFTED ? 1.0f + tot : tot;
   const float jx = d1 + (d7 + d9) + (d11 + d13);
   const float jy = d3 + (d7 - d9) + (d15 + d17);
   const float jz = d5 + (d11 - d13) + (d15 - d17);
@@ -222,12 +247,12 @@ __device__ __forceinline__ void collide_fast(const float (&f)[19], uint32_t cls,
     // Zou/He density from populations with c_z <= 0 (src/engine.js:282-284)
     const float s0 = f[0] + s1 + s3 + sxy;
     const float sm = f[6] + f[12] + f[13] + f[16] + f[17];
-    r = rho = (s0 + 2.0f * sm) / (1.0f - P.u0);
+    r = rho = (SHIFTED ? 1.0f + (s0 + 2.0f * sm) : s0 + 2.0f * sm) / (1.0f - P.u0);
     vx = ux = 0.0f; vy = uy = 0.0f; vz = uz = P.u0;
   } else if (cls == kClsOutlet) {
     r = rho = 1.0f;
   } else {
-    const float r3 = rho * (1.0f / 3.0f);
+    const float r3 = (SHIFTED ? tot : rho) * (1.0f / 3.0f);
     const float nxx = (s1 + sxy + sxz) - r3 - jx * ux;
     const float nyy = (s3 + sxy + syz) - r3 - jy * uy;
     const float nzz = (s5 + sxz + syz) - r3 - jz * uz;
@@ -247,9 +272,10 @@ __device__ __forceinline__ void collide_fast(const float (&f)[19], uint32_t cls,
   const float base = 1.0f - 1.5f * (vx * vx + vy * vy + vz * vz);
   const float w1 = r * (1.0f / 18.0f), w2 = r * (1.0f / 36.0f);
   const float keep = 1.0f - nsv;
-  // one opposite pair: equilibrium = even +- odd, then relax both
-  auto pair = [&](int q, float cu, float w) {
-    const float even = w * fmaf(4.5f * cu, cu, base), odd = (3.0f * w) * cu;
+  // one opposite pair: equilibrium = even +- odd (SHIFTED: minus the pair's weight W), then relax both
+  auto pair = [&](int q, float cu, float w, float W) {
+    const float even = SHIFTED ? fmaf(w, fmaf(4.5f * cu, cu, base), -W) : w * fmaf(4.5f * cu, cu, base);
+    const float odd = (3.0f * w) * cu;
     const float ep = even + odd, em = even - odd;
     const float bp = fmaf(omega, ep - f[q], f[q]), bm = fmaf(omega, em - f[q + 1], f[q + 1]);
     if (HAS_NS) {
@@ -260,13 +286,14 @@ __device__ __forceinline__ void collide_fast(const float (&f)[19], uint32_t cls,
     }
   };
   {
-    const float e0 = r * (1.0f / 3.0f) * base;
+    const float e0 = SHIFTED ? fmaf(r * (1.0f / 3.0f), base, -1.0f / 3.0f) : r * (1.0f / 3.0f) * base;
     const float b0 = fmaf(omega, e0 - f[0], f[0]);
     fo[0] = HAS_NS ? keep * b0 + nsv * f[0] : b0;
   }
-  pair(1, vx, w1); pair(3, vy, w1); pair(5, vz, w1);
-  pair(7, vx + vy, w2); pair(9, vx - vy, w2); pair(11, vx + vz, w2);
-  pair(13, vx - vz, w2); pair(15, vy + vz, w2); pair(17, vy - vz, w2);
+  constexpr float W1 = 1.0f / 18.0f, W2 = 1.0f / 36.0f;
+  pair(1, vx, w1, W1); pair(3, vy, w1, W1); pair(5, vz, w1, W1);
+  pair(7, vx + vy, w2, W2); pair(9, vx - vy, w2, W2); pair(11, vx + vz, w2, W2);
+  pair(13, vx - vz, w2, W2); pair(15, vy + vz, w2, W2); pair(17, vy - vz, w2, W2);
   if (HAS_NS) { ux *= keep; uy *= keep; uz *= keep; }
 }
 

@@ -84,10 +84,10 @@ __device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, cons
       // directions are then bounced back from the cell's own slot.
 #pragma unroll
       for (int q = 0; q < 19; q++)
-        fi[j][q] = S::ld(f + ((uint32_t)opp(q) * Np + p[j] - (uint32_t)a.off[q]), weight<L>(q));
+        fi[j][q] = S::ldr(f + ((uint32_t)opp(q) * Np + p[j] - (uint32_t)a.off[q]));
     } else {
 #pragma unroll
-      for (int q = 0; q < 19; q++) fi[j][q] = S::ld(f + ((uint32_t)q * Np + p[j]), weight<L>(q));
+      for (int q = 0; q < 19; q++) fi[j][q] = S::ldr(f + ((uint32_t)q * Np + p[j]));
     }
     // running sums of the averages: loaded now, in flight with the populations
     if (ACC) {
@@ -101,13 +101,14 @@ __device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, cons
     if (ODD && m[j] != 0x7FFFFu) {
 #pragma unroll
       for (int q = 1; q < 19; q++)
-        if (!((m[j] >> q) & 1u)) fi[j][q] = S::ld(f + ((uint32_t)q * Np + p[j]), weight<L>(q));
+        if (!((m[j] >> q) & 1u)) fi[j][q] = S::ldr(f + ((uint32_t)q * Np + p[j]));
     }
     const uint32_t cls = (m[j] >> kClassShift) & 3u;
     L nsv = (L)0;
     if (HAS_NS) nsv = (L)a.ns[p[j]];
     L fo[19], ux, uy, uz, rho;
-    if constexpr (sizeof(L) == 4) collide_fast<HAS_NS>(fi[j], cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
+    if constexpr (sizeof(L) == 4)
+      collide_fast<HAS_NS, S::kShifted>(fi[j], cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
     else collide<L, HAS_NS>(fi[j], cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
 #pragma unroll
     for (int q = 0; q < 19; q++) {
@@ -115,7 +116,7 @@ __device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, cons
       if (ODD)
         idx = ((m[j] >> opp(q)) & 1u) ? (uint32_t)q * Np + p[j] + (uint32_t)a.off[q] : (uint32_t)opp(q) * Np + p[j];
       else idx = (uint32_t)opp(q) * Np + p[j];
-      S::st(f + idx, fo[q], weight<L>(q));
+      S::str(f + idx, fo[q]);
     }
     if (ACC) {
       Acc *acc = (Acc *)a.acc;

@@ -264,27 +264,27 @@ __global__ void __launch_bounds__(kTmaThreads, 2)
       for (int q = 0; q < 19; q++) {
         if (ODD) {
           const T *row = (const T *)((const unsigned char *)sp + G::slot_off(q));
-          fi[q] = S::lds(row + (cz(q) == 0 ? lane : G::kPad + lane - cz(q)), weight<L>(q));
+          fi[q] = S::ldsr(row + (cz(q) == 0 ? lane : G::kPad + lane - cz(q)));
         } else {
-          fi[q] = S::lds(sp + q * 32 + lane, weight<L>(q));
+          fi[q] = S::ldsr(sp + q * 32 + lane);
         }
       }
       if (ODD && m != 0x7FFFFu) {
 #pragma unroll
         for (int q = 1; q < 19; q++)
-          if (!((m >> q) & 1u)) fi[q] = S::ld(f + ((uint32_t)q * Np + p), weight<L>(q));  // bounce-back
+          if (!((m >> q) & 1u)) fi[q] = S::ldr(f + ((uint32_t)q * Np + p));  // bounce-back
       }
       const uint32_t cls = (m >> kClassShift) & 3u;
       L nsv = (L)0;
       if (HAS_NS) nsv = (L)a.ns[p];
       L fo[19], ux, uy, uz, rho;
-      collide_fast<HAS_NS>(fi, cls, nsv, CP, fo, ux, uy, uz, rho);
+      collide_fast<HAS_NS, S::kShifted>(fi, cls, nsv, CP, fo, ux, uy, uz, rho);
 #pragma unroll
       for (int q = 0; q < 19; q++) {
         uint32_t idx;
         if (ODD) idx = ((m >> opp(q)) & 1u) ? (uint32_t)q * Np + p + (uint32_t)a.off[q] : (uint32_t)opp(q) * Np + p;
         else idx = (uint32_t)opp(q) * Np + p;
-        S::st(f + idx, fo[q], weight<L>(q));
+        S::str(f + idx, fo[q]);
       }
       if (ACC) {
         const float *ac = (const float *)(base + ST::kAccOff + warp * 512);
