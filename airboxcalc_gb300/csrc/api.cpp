@@ -1651,13 +1651,19 @@ extern "C" int abx_batch_get_info(const abx_batch *b, abx_batch_info *o) {
 }
 
 // ------------------------------------------------------------------ post-processing
-static PostArgs post_args(const abx_sim &s) {
+// Arguments of the post-processing kernels, with the float32 averages made into `avg` (4 * Np floats).
+static int post_args(abx_sim &s, DevBuf &avg, PostArgs *out, const char *what) {
   const abx_geom &g = *s.g;
   PostArgs a{};
   a.nx = g.nx; a.ny = g.ny; a.nz = g.nz; a.nzp = g.nzp; a.kpad = g.kpad; a.Np = g.Np;
   a.mask = g.d_mask; a.ns = s.has_ns ? s.d_ns : nullptr; a.opening = g.d_opening;
   a.acc = s.d_acc; a.acc_double = s.p.storage == ABX_STORE_F64; a.dn = s.nacc > 1 ? s.nacc : 1; a.u0 = s.u0;
-  return a;
+  CK(cudaMalloc(&avg.p, sizeof(float) * 4 * (size_t)g.Np), what);
+  a.avg = (const float *)avg.p;
+  CK(post_average(a, (float *)avg.p, s.st), what);
+  s.launches++;
+  *out = a;
+  return ABX_OK;
 }
 
 static int find_index_ge(const std::vector<float> &a, double v) {  // Array#findIndex(z => z >= v)
@@ -1686,7 +1692,10 @@ extern "C" int abx_sim_field3d(abx_sim *s, float *spd, float *pst, float *loss, 
     int k = 0;
     for (int i = 0; i < 3; i++) if (host[i]) o[i] = (float *)out.p + N * k++;
   }
-  CK(post_field3d(post_args(*s), kB, jb, (double *)scal.p, o[0], o[1], o[2], s->st), "sim_field3d");
+  DevBuf avg;
+  PostArgs pa;
+  if (int rc = post_args(*s, avg, &pa, "sim_field3d")) return rc;
+  CK(post_field3d(pa, kB, jb, (double *)scal.p, o[0], o[1], o[2], s->st), "sim_field3d");
   s->launches += 2;
   double sc[2];
   CK(cudaMemcpyAsync(sc, scal.p, sizeof sc, cudaMemcpyDeviceToHost, s->st), "sim_field3d");
@@ -1719,7 +1728,10 @@ extern "C" int abx_sim_planes(abx_sim *s, float *out, abx_planes_info *info) {
   if (out) {
     DevBuf d;
     CK(cudaMalloc(&d.p, sizeof(float) * n), "sim_planes");
-    CK(post_planes(post_args(*s), ic, jc, jlow, (float *)d.p, s->st), "sim_planes");
+    DevBuf avg;
+    PostArgs pa;
+    if (int rc = post_args(*s, avg, &pa, "sim_planes")) return rc;
+    CK(post_planes(pa, ic, jc, jlow, (float *)d.p, s->st), "sim_planes");
     s->launches++;
     CK(cudaMemcpyAsync(out, d.p, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st), "sim_planes");
     CK(cudaStreamSynchronize(s->st), "sim_planes");
@@ -1764,7 +1776,10 @@ extern "C" int abx_sim_streamlines(abx_sim *s, int max_seeds, float *pts, float 
     CK(cudaMalloc(&dpts.p, sizeof(double) * P.size()), "sim_streamlines");
     CK(cudaMalloc(&dcnt.p, sizeof(int) * nsel), "sim_streamlines");
     CK(cudaMemcpyAsync(dseeds.p, sel.data(), sizeof(double) * sel.size(), cudaMemcpyHostToDevice, s->st), "sim_streamlines");
-    CK(post_streamlines(post_args(*s), (const double *)dseeds.p, nsel, g.top, (double *)dpts.p, (int *)dcnt.p, s->st),
+    DevBuf avg;
+    PostArgs pa;
+    if (int rc = post_args(*s, avg, &pa, "sim_streamlines")) return rc;
+    CK(post_streamlines(pa, (const double *)dseeds.p, nsel, g.top, (double *)dpts.p, (int *)dcnt.p, s->st),
        "sim_streamlines");
     s->launches++;
     CK(cudaMemcpyAsync(cnt.data(), dcnt.p, sizeof(int) * nsel, cudaMemcpyDeviceToHost, s->st), "sim_streamlines");

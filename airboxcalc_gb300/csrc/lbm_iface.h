@@ -179,8 +179,11 @@ struct PostArgs {
   int acc_double;            // sums in float64 (the float64 run)
   double dn;                 // averaged steps (>= 1)
   double u0;
+  const float *avg;          // [4][Np] averages as float32 (post_average), read by the kernels below
 };
 constexpr int kMaxLinePoints = 2001;   // points one streamline can keep (6000 steps, every 3rd, plus the last)
+// the float32 averages sum / nacc of every padded cell into avg (4 * Np floats)
+cudaError_t post_average(const PostArgs &a, float *avg, cudaStream_t st);
 // field3d: d_scal receives pin and rhoRef; spd/pst/loss (nx*ny*nz floats, may be null)
 cudaError_t post_field3d(const PostArgs &a, int kB, int jb, double *d_scal, float *spd, float *pst, float *loss,
                          cudaStream_t st);

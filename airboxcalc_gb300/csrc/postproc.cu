@@ -8,7 +8,7 @@
 //                the inlet opening, one thread per seed
 //
 // The averages are read as the reference holds them: the Float32Array of
-// simulate() (sum / nacc rounded to float32, :356).  Sums the reference takes
+// simulate() (sum / nacc rounded to float32, :356), made once per call.  Sums the reference takes
 // in one loop (the inlet's mass-weighted total pressure, the reference
 // density under the filter) run in one thread, in its order.  Math.hypot
 // follows V8's published algorithm (scale by the largest magnitude,
@@ -20,14 +20,18 @@
 
 namespace abx {
 
+// The averages as the reference holds them, sum / nacc rounded to float32 (a Float32Array, :356),
+// computed once per call into a float array that the kernels below read.
 template <typename Acc>
+__global__ void average_kernel(const Acc *__restrict__ acc, int64_t n, double dn, float *__restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (float)((double)acc[i] / dn);
+}
+
 struct AvgView {
-  const Acc *acc;
+  const float *avg;
   int64_t Np;
-  double dn;
-  __device__ __forceinline__ double operator()(int comp, int64_t p) const {
-    return (double)(float)((double)acc[comp * Np + p] / dn);
-  }
+  __device__ __forceinline__ double operator()(int comp, int64_t p) const { return (double)avg[comp * Np + p]; }
 };
 
 __device__ __forceinline__ double js_hypot3(double x, double y, double z) {
@@ -65,9 +69,8 @@ __device__ __forceinline__ int64_t padded(const PostArgs &a, int i, int j, int k
 
 // out[0] = pin (mass-flow-weighted total pressure at k = kB over the opening, :705-711),
 // out[1] = rhoRef (mean density on layer jb, :658-659)
-template <typename Acc>
 __global__ void post_scalars_kernel(const PostArgs a, int kB, int jb, double *out) {
-  const AvgView<Acc> U{(const Acc *)a.acc, a.Np, a.dn};
+  const AvgView U{a.avg, a.Np};
   // loads issued unconditionally (every index is inside the arrays) so that the loop pipelines; the sums
   // still take the cells in the reference's order
   double pb = 0;
@@ -96,9 +99,8 @@ __global__ void post_scalars_kernel(const PostArgs a, int kB, int jb, double *ou
   out[1] = pb / pbN;
 }
 
-template <typename Acc>
 __global__ void field3d_kernel(const PostArgs a, int kB, const double *scal, float *spd, float *pst, float *loss) {
-  const AvgView<Acc> U{(const Acc *)a.acc, a.Np, a.dn};
+  const AvgView U{a.avg, a.Np};
   const int64_t N = (int64_t)a.nx * a.ny * a.nz;
   const double q = 0.5 * a.u0 * a.u0, pin = scal[0], rhoRef = scal[1];
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
@@ -120,9 +122,8 @@ __global__ void field3d_kernel(const PostArgs a, int kB, const double *scal, flo
 
 // planInlet (j = jc), planLow (j = jlow): speed, ua = ux/u0, ub = uz/u0 over (i, k);
 // lon (i = ic): speed, ua = uz/u0, ub = uy/u0 over (k, j).
-template <typename Acc>
 __global__ void planes_kernel(const PostArgs a, int ic, int jc, int jlow, float *out) {
-  const AvgView<Acc> U{(const Acc *)a.acc, a.Np, a.dn};
+  const AvgView U{a.avg, a.Np};
   const int64_t P = (int64_t)a.nx * a.nz, Q = (int64_t)a.nz * a.ny, n = 2 * P + Q;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
     float *s, *ua, *ub;
@@ -146,8 +147,7 @@ __global__ void planes_kernel(const PostArgs a, int ic, int jc, int jlow, float 
   }
 }
 
-template <typename Acc>
-__device__ double trace_vel(const PostArgs &a, const AvgView<Acc> &U, double x, double y, double z, double out[3]) {
+__device__ double trace_vel(const PostArgs &a, const AvgView &U, double x, double y, double z, double out[3]) {
   const double fi0 = floor(x), fj0 = floor(y), fk0 = floor(z);
   const double fx = x - fi0, fy = y - fj0, fz = z - fk0;
   const int i0 = (int)fi0, j0 = (int)fj0, k0 = (int)fk0;
@@ -177,12 +177,11 @@ __device__ __forceinline__ bool trace_inside(const PostArgs &a, double x, double
 
 // One thread per seed: the trace of :739-751, up to kMaxLinePoints points (x, y, z, |u|/u0) in
 // grid-cell coordinates into the seed's slot; count[s] = points kept.
-template <typename Acc>
 __global__ void streamline_kernel(const PostArgs a, const double *seeds, int nseeds, int top, double *pts,
                                   int *count) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseeds) return;
-  const AvgView<Acc> U{(const Acc *)a.acc, a.Np, a.dn};
+  const AvgView U{a.avg, a.Np};
   double x = seeds[3 * s], y = seeds[3 * s + 1], z = seeds[3 * s + 2], v1[3], v2[3];
   double *P = pts + (int64_t)s * 4 * kMaxLinePoints;
   const double ds = 0.35;
@@ -210,23 +209,24 @@ static unsigned grid_of(int64_t n) {
   return (unsigned)(b < 1 ? 1 : b);
 }
 
+cudaError_t post_average(const PostArgs &a, float *avg, cudaStream_t st) {
+  const int64_t n = 4 * a.Np;
+  if (a.acc_double) average_kernel<double><<<grid_of(n), 256, 0, st>>>((const double *)a.acc, n, a.dn, avg);
+  else average_kernel<float><<<grid_of(n), 256, 0, st>>>((const float *)a.acc, n, a.dn, avg);
+  return cudaGetLastError();
+}
+
 cudaError_t post_field3d(const PostArgs &a, int kB, int jb, double *d_scal, float *spd, float *pst, float *loss,
                          cudaStream_t st) {
   const int64_t N = (int64_t)a.nx * a.ny * a.nz;
-  if (a.acc_double) {
-    post_scalars_kernel<double><<<1, 1, 0, st>>>(a, kB, jb, d_scal);
-    field3d_kernel<double><<<grid_of(N), 256, 0, st>>>(a, kB, d_scal, spd, pst, loss);
-  } else {
-    post_scalars_kernel<float><<<1, 1, 0, st>>>(a, kB, jb, d_scal);
-    field3d_kernel<float><<<grid_of(N), 256, 0, st>>>(a, kB, d_scal, spd, pst, loss);
-  }
+  post_scalars_kernel<<<1, 1, 0, st>>>(a, kB, jb, d_scal);
+  field3d_kernel<<<grid_of(N), 256, 0, st>>>(a, kB, d_scal, spd, pst, loss);
   return cudaGetLastError();
 }
 
 cudaError_t post_planes(const PostArgs &a, int ic, int jc, int jlow, float *out, cudaStream_t st) {
   const int64_t n = 2 * (int64_t)a.nx * a.nz + (int64_t)a.nz * a.ny;
-  if (a.acc_double) planes_kernel<double><<<grid_of(n), 256, 0, st>>>(a, ic, jc, jlow, out);
-  else planes_kernel<float><<<grid_of(n), 256, 0, st>>>(a, ic, jc, jlow, out);
+  planes_kernel<<<grid_of(n), 256, 0, st>>>(a, ic, jc, jlow, out);
   return cudaGetLastError();
 }
 
@@ -234,8 +234,7 @@ cudaError_t post_streamlines(const PostArgs &a, const double *seeds, int nseeds,
                              cudaStream_t st) {
   if (nseeds <= 0) return cudaSuccess;
   const unsigned blocks = (unsigned)((nseeds + 31) / 32);
-  if (a.acc_double) streamline_kernel<double><<<blocks, 32, 0, st>>>(a, seeds, nseeds, top, pts, count);
-  else streamline_kernel<float><<<blocks, 32, 0, st>>>(a, seeds, nseeds, top, pts, count);
+  streamline_kernel<<<blocks, 32, 0, st>>>(a, seeds, nseeds, top, pts, count);
   return cudaGetLastError();
 }
 
