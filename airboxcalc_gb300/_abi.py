@@ -91,7 +91,7 @@ class Timing(C.Structure):
 
 class NetParams(C.Structure):
     _fields_ = [("res", C.c_int), ("base", C.c_int), ("levels", C.c_int), ("device", C.c_int),
-                ("seed", C.c_ulonglong)]
+                ("seed", C.c_ulonglong), ("coords", C.c_int)]
 
 
 class NetInfo(C.Structure):

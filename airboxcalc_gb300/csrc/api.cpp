@@ -1111,7 +1111,7 @@ extern "C" int abx_net_create(const abx_net_params *p, abx_net **out) {
   if (p->device < 0 || p->device >= nd) return fail(ABX_ERR_INVALID_ARGUMENT, "net_create: no device %d", p->device);
   std::unique_ptr<abx_net> n(new abx_net());
   n->net.device = p->device;
-  cudaError_t e = n->net.init(R, p->base, L, p->device, p->seed);
+  cudaError_t e = n->net.init(R, p->base, L, p->device, p->seed, p->coords != 0);
   if (e != cudaSuccess) return cuda_fail(e, "net_create");
   *out = n.release();
   return ABX_OK;
@@ -1123,7 +1123,7 @@ extern "C" int abx_net_get_info(const abx_net *n, abx_net_info *o) {
   if (!n || !o) return fail(ABX_ERR_INVALID_ARGUMENT, "net_get_info: null argument");
   std::memset(o, 0, sizeof *o);
   o->res = n->net.R; o->base = n->net.base; o->levels = n->net.levels;
-  o->in_channels = WarmNet::kIn; o->out_channels = WarmNet::kOut;
+  o->in_channels = n->net.n_in; o->out_channels = WarmNet::kOut;
   o->n_samples = (int)n->net.samples.size(); o->n_params = n->net.n_params;
   return ABX_OK;
 }
@@ -1183,9 +1183,9 @@ extern "C" int abx_net_get_sample(abx_net *n, int i, float *x, float *t, float *
   const int64_t V = n->net.voxels();
   const float *b = n->net.samples[i].buf;
   CK(cudaSetDevice(n->net.device), "net_get_sample");
-  if (x) CK(cudaMemcpyAsync(x, b, sizeof(float) * WarmNet::kIn * V, cudaMemcpyDeviceToHost, n->net.st), "net_get_sample");
-  if (t) CK(cudaMemcpyAsync(t, b + WarmNet::kIn * V, sizeof(float) * WarmNet::kOut * V, cudaMemcpyDeviceToHost, n->net.st), "net_get_sample");
-  if (m) CK(cudaMemcpyAsync(m, b + (WarmNet::kIn + WarmNet::kOut) * V, sizeof(float) * V, cudaMemcpyDeviceToHost, n->net.st), "net_get_sample");
+  if (x) CK(cudaMemcpyAsync(x, b, sizeof(float) * n->net.n_in * V, cudaMemcpyDeviceToHost, n->net.st), "net_get_sample");
+  if (t) CK(cudaMemcpyAsync(t, b + (int64_t)n->net.n_in * V, sizeof(float) * WarmNet::kOut * V, cudaMemcpyDeviceToHost, n->net.st), "net_get_sample");
+  if (m) CK(cudaMemcpyAsync(m, b + (int64_t)(n->net.n_in + WarmNet::kOut) * V, sizeof(float) * V, cudaMemcpyDeviceToHost, n->net.st), "net_get_sample");
   CK(cudaStreamSynchronize(n->net.st), "net_get_sample");
   return ABX_OK;
 }
@@ -1223,7 +1223,7 @@ extern "C" int abx_net_forward_backward(abx_net *n, const float *d_x, const floa
   CK(cudaSetDevice(w.device), "net_forward_backward");
   CK(w.ensure_batch(B), "net_forward_backward");
   const int64_t V = w.voxels();
-  CK(cudaMemcpyAsync(w.input(), d_x, sizeof(float) * B * WarmNet::kIn * V, cudaMemcpyDeviceToDevice, w.st), "net_forward_backward");
+  CK(cudaMemcpyAsync(w.input(), d_x, sizeof(float) * B * w.n_in * V, cudaMemcpyDeviceToDevice, w.st), "net_forward_backward");
   CK(w.forward(B), "net_forward_backward");
   CK(w.loss(B, d_t, d_m, scale, d_grad != nullptr, loss), "net_forward_backward");
   CK(cudaMemcpyAsync(d_pred, w.output(), sizeof(float) * B * WarmNet::kOut * V, cudaMemcpyDeviceToDevice, w.st), "net_forward_backward");
@@ -1248,7 +1248,7 @@ extern "C" int abx_net_predict(abx_net *n, abx_sim *s, float *features, float *p
   if (int rc = net_infer(n, s)) return rc;
   WarmNet &w = n->net;
   const int64_t V = w.voxels();
-  if (features) CK(cudaMemcpyAsync(features, w.input(), sizeof(float) * WarmNet::kIn * V, cudaMemcpyDeviceToHost, w.st), "net_predict");
+  if (features) CK(cudaMemcpyAsync(features, w.input(), sizeof(float) * w.n_in * V, cudaMemcpyDeviceToHost, w.st), "net_predict");
   if (pred) CK(cudaMemcpyAsync(pred, w.output(), sizeof(float) * WarmNet::kOut * V, cudaMemcpyDeviceToHost, w.st), "net_predict");
   CK(cudaStreamSynchronize(w.st), "net_predict");
   return ABX_OK;

@@ -203,6 +203,8 @@ struct GridDesc {
 };
 // Network input (9 x R^3 floats), with two R^3 int scratch arrays for the jump flood.
 cudaError_t ws_features(const GridDesc &g, int R, float K, float *out, int *seed_a, int *seed_b, cudaStream_t st);
+// Voxel coordinates (3 x R^3: (a + 0.5) / R along x, y, z).
+cudaError_t ws_coords(int R, float *out, cudaStream_t st);
 // Training target (4 x R^3) and loss weight (R^3) from a run's averages.
 cudaError_t ws_targets(const GridDesc &g, int storage, const void *acc, int nacc, double u0, int R, float *t, float *m,
                        cudaStream_t st);

@@ -38,8 +38,9 @@ void WarmNet::clear_samples() {
   samples.clear();
 }
 
-cudaError_t WarmNet::init(int R_, int base_, int levels_, int device_, uint64_t seed) {
+cudaError_t WarmNet::init(int R_, int base_, int levels_, int device_, uint64_t seed, bool coords) {
   R = R_; base = base_; levels = levels_; device = device_;
+  n_in = kGeomIn + (coords ? 3 : 0);
   NCK(cudaSetDevice(device));
   NCK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   auto add_tensor = [&](int C, int D) {
@@ -58,7 +59,7 @@ cudaError_t WarmNet::init(int R_, int base_, int levels_, int device_, uint64_t 
     return out;
   };
   auto ch = [&](int l) { return base << l; };
-  int t = add_tensor(kIn, R);
+  int t = add_tensor(n_in, R);
   std::vector<int> skip(levels);
   for (int l = 0; l < levels; l++) {
     t = add_conv(t, ch(l), l == 0 ? 1 : 2, 1);
@@ -173,19 +174,21 @@ cudaError_t WarmNet::loss(int B, const float *t, const float *m, double scale, b
 }
 
 cudaError_t WarmNet::features(const GridDesc &g, float K, float *dst) {
-  return ws_features(g, R, K, dst, d_seed, d_seed + voxels(), st);
+  NCK(ws_features(g, R, K, dst, d_seed, d_seed + voxels(), st));
+  if (n_in > kGeomIn) NCK(ws_coords(R, dst + (int64_t)kGeomIn * voxels(), st));
+  return cudaSuccess;
 }
 
 cudaError_t WarmNet::add_sample(const GridDesc &g, float K, int storage, const void *acc, int nacc, double u0) {
   NCK(cudaSetDevice(device));
   const int64_t V = voxels();
   Sample s;
-  NCK(cudaMalloc(&s.buf, sizeof(float) * (kIn + kOut + 1) * V));
+  NCK(cudaMalloc(&s.buf, sizeof(float) * (n_in + kOut + 1) * V));
   cudaError_t e = features(g, K, s.buf);
-  if (e == cudaSuccess) e = ws_targets(g, storage, acc, nacc, u0, R, s.buf + kIn * V, s.buf + (kIn + kOut) * V, st);
+  if (e == cudaSuccess) e = ws_targets(g, storage, acc, nacc, u0, R, s.buf + (int64_t)n_in * V, s.buf + (int64_t)(n_in + kOut) * V, st);
   std::vector<float> m(V);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(m.data(), s.buf + (kIn + kOut) * V, sizeof(float) * V, cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(m.data(), s.buf + (int64_t)(n_in + kOut) * V, sizeof(float) * V, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) { cudaFree(s.buf); return e; }
   for (float v : m) s.msum += v;
@@ -196,13 +199,13 @@ cudaError_t WarmNet::add_sample(const GridDesc &g, float K, int storage, const v
 cudaError_t WarmNet::stage(int idx, int b, bool flip) {
   const int64_t V = voxels();
   const Sample &s = samples[idx];
-  NCK(cudaMemcpyAsync(input(b), s.buf, sizeof(float) * kIn * V, cudaMemcpyDeviceToDevice, st));
-  NCK(cudaMemcpyAsync(d_bt + (int64_t)b * kOut * V, s.buf + kIn * V, sizeof(float) * kOut * V,
+  NCK(cudaMemcpyAsync(input(b), s.buf, sizeof(float) * n_in * V, cudaMemcpyDeviceToDevice, st));
+  NCK(cudaMemcpyAsync(d_bt + (int64_t)b * kOut * V, s.buf + (int64_t)n_in * V, sizeof(float) * kOut * V,
                       cudaMemcpyDeviceToDevice, st));
-  NCK(cudaMemcpyAsync(d_bm + (int64_t)b * V, s.buf + (kIn + kOut) * V, sizeof(float) * V, cudaMemcpyDeviceToDevice,
+  NCK(cudaMemcpyAsync(d_bm + (int64_t)b * V, s.buf + (int64_t)(n_in + kOut) * V, sizeof(float) * V, cudaMemcpyDeviceToDevice,
                       st));
   if (flip) {
-    NCK(ws_flip_x(input(b), kIn, R, -1, st));
+    NCK(ws_flip_x(input(b), kGeomIn, R, -1, st));   // the coordinate channels stay: the mirrored box's own
     NCK(ws_flip_x(d_bt + (int64_t)b * kOut * V, kOut, R, 0, st));
     NCK(ws_flip_x(d_bm + (int64_t)b * V, 1, R, -1, st));
   }

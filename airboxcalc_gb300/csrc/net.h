@@ -11,7 +11,7 @@
 //   head     conv(c0 -> 4), no activation
 // Every conv is 3x3x3 with padding 1 and a ReLU except the head.
 // Input channels: fluid, inlet, outlet, filter fraction, wall distance, K,
-// grid extent (3); output: u / u0 (3) and (rho - 1) / (5 u0^2).
+// grid extent (3), optionally the voxel's coordinates (3); output: u / u0 (3) and (rho - 1) / (5 u0^2).
 #pragma once
 #include <cuda_runtime_api.h>
 #include <stdint.h>
@@ -25,14 +25,15 @@ namespace abx {
 
 class WarmNet {
  public:
-  static constexpr int kIn = 9, kOut = 4;
+  static constexpr int kGeomIn = 9, kOut = 4;   // geometry channels, output channels
 
   struct Conv { int cin, cout, stride, relu; int64_t w_off, b_off; };
   struct Tensor { int C, D; int64_t off; };           // C x D^3 floats per sample, at cap_B * off
   struct Node { int kind, in, in2, out, conv; };      // kind: 0 conv, 1 upsample, 2 add
-  struct Sample { float *buf = nullptr; double msum = 0; };   // [9 V | 4 V | V]
+  struct Sample { float *buf = nullptr; double msum = 0; };   // [n_in V | 4 V | V]
 
   int R = 0, base = 0, levels = 0, device = 0;
+  int n_in = kGeomIn;                                 // + 3 voxel-coordinate channels when enabled
   cudaStream_t st = nullptr;
   std::vector<Conv> convs;
   std::vector<Tensor> tensors;
@@ -51,7 +52,7 @@ class WarmNet {
 
   ~WarmNet();
   // Builds the layer list, allocates the parameters and initialises them from `seed`.
-  cudaError_t init(int R, int base, int levels, int device, uint64_t seed);
+  cudaError_t init(int R, int base, int levels, int device, uint64_t seed, bool coords = false);
   int64_t voxels() const { return (int64_t)R * R * R; }
   float *tensor(int t, int b = 0) const { return d_act + tensors[t].off * cap_B + (int64_t)b * tensors[t].C * tensors[t].D * tensors[t].D * tensors[t].D; }
   float *grad(int t, int b = 0) const { return d_grad + tensors[t].off * cap_B + (int64_t)b * tensors[t].C * tensors[t].D * tensors[t].D * tensors[t].D; }

@@ -228,6 +228,21 @@ cudaError_t ws_features(const GridDesc &g, int R, float K, float *out, int *seed
   return cudaGetLastError();
 }
 
+__global__ void coords_kernel(int R, float *__restrict__ out) {
+  const int V = R * R * R;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const int c = v % R, b = (v / R) % R, a = v / (R * R);
+    out[v] = (a + 0.5f) / R;
+    out[V + v] = (b + 0.5f) / R;
+    out[2 * V + v] = (c + 0.5f) / R;
+  }
+}
+
+cudaError_t ws_coords(int R, float *out, cudaStream_t st) {
+  coords_kernel<<<grid_for((int64_t)R * R * R), 256, 0, st>>>(R, out);
+  return cudaGetLastError();
+}
+
 cudaError_t ws_targets(const GridDesc &g, int storage, const void *acc, int nacc, double u0, int R, float *t, float *m,
                        cudaStream_t st) {
   const double inv_n = 1.0 / (nacc > 1 ? nacc : 1);

@@ -47,13 +47,15 @@ def variant(seed: int, dx: float = 2.0):
 class Net:
     """The warm-start network on one GPU (abx_net)."""
 
-    def __init__(self, res: int = 64, base: int = 16, levels: int = 4, device: int = 0, seed: int = 0):
-        p = A.NetParams(res=res, base=base, levels=levels, device=device, seed=seed)
+    def __init__(self, res: int = 64, base: int = 16, levels: int = 4, device: int = 0, seed: int = 0,
+                 coords: bool = False):
+        p = A.NetParams(res=res, base=base, levels=levels, device=device, seed=seed, coords=1 if coords else 0)
         h = C.c_void_p()
         E._check(A.load().abx_net_create(C.byref(p), C.byref(h)))
         self._h = h
-        self.res, self.base, self.levels = res, base, levels
+        self.res, self.base, self.levels, self.coords = res, base, levels, bool(coords)
         self.V = res ** 3
+        self.n_in = 12 if coords else 9
 
     @property
     def info(self) -> dict:
@@ -79,12 +81,13 @@ class Net:
     def save(self, path: str, **meta):
         os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
         np.savez_compressed(path, weights=self.get_weights(), res=self.res, base=self.base, levels=self.levels,
-                            meta=json.dumps(meta))
+                            coords=int(self.coords), meta=json.dumps(meta))
 
     @classmethod
     def load(cls, path: str = WEIGHTS, device: int = 0) -> "Net":
         d = np.load(path)
-        n = cls(int(d["res"]), int(d["base"]), int(d["levels"]), device=device)
+        n = cls(int(d["res"]), int(d["base"]), int(d["levels"]), device=device,
+                coords=bool(int(d["coords"])) if "coords" in d else False)
         n.set_weights(d["weights"])
         n.meta = json.loads(str(d["meta"])) if "meta" in d else {}
         return n
@@ -97,12 +100,12 @@ class Net:
 
     def sample(self, i: int):
         V = self.V
-        x = np.empty(9 * V, np.float32)
+        x = np.empty(self.n_in * V, np.float32)
         t = np.empty(4 * V, np.float32)
         m = np.empty(V, np.float32)
         E._check(A.load().abx_net_get_sample(self._h, i, E._ptr(x), E._ptr(t), E._ptr(m)))
         r = self.res
-        return x.reshape(9, r, r, r), t.reshape(4, r, r, r), m.reshape(r, r, r)
+        return x.reshape(self.n_in, r, r, r), t.reshape(4, r, r, r), m.reshape(r, r, r)
 
     def train(self, first: int, count: int, epochs: int, batch: int = 8, lr: float = 1e-3, lr_min: float = 1e-5,
               seed: int = 0, flip: bool = True) -> np.ndarray:
@@ -128,10 +131,10 @@ class Net:
 
     def predict(self, sim: E.Simulation):
         r = self.res
-        x = np.empty(9 * self.V, np.float32)
+        x = np.empty(self.n_in * self.V, np.float32)
         y = np.empty(4 * self.V, np.float32)
         E._check(A.load().abx_net_predict(self._h, sim._h, E._ptr(x), E._ptr(y)))
-        return x.reshape(9, r, r, r), y.reshape(4, r, r, r)
+        return x.reshape(self.n_in, r, r, r), y.reshape(4, r, r, r)
 
     def __del__(self):
         try:
@@ -218,6 +221,7 @@ def main(argv=None):
     ap.add_argument("--res", type=int, default=64)
     ap.add_argument("--base", type=int, default=16)
     ap.add_argument("--levels", type=int, default=4)
+    ap.add_argument("--coords", action="store_true", help="add the voxel coordinates as input channels")
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1e-3)
@@ -226,7 +230,7 @@ def main(argv=None):
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--log", default=None, help="JSON-lines log of the generated samples")
     a = ap.parse_args(argv)
-    net = Net(a.res, a.base, a.levels, seed=a.seed)
+    net = Net(a.res, a.base, a.levels, seed=a.seed, coords=a.coords)
     logf = open(a.log, "w") if a.log else None
     t0 = time.perf_counter()
 

@@ -272,8 +272,8 @@ int abx_voxelize_static(const float *d_tris, size_t nfloats, const double origin
  *
  * The network is a 3-D convolutional encoder-decoder on an R^3 resampling
  * of the grid (levels L, channels base << l).  Input: fluid / inlet /
- * outlet / filter fraction of each voxel's footprint, wall distance, K and
- * the grid extent; output: the time-averaged u / u0 and (rho - 1)/(5 u0^2).
+ * outlet / filter fraction of each voxel's footprint, wall distance, K,
+ * the grid extent (and optionally the voxel's coordinates); output: the time-averaged u / u0 and (rho - 1)/(5 u0^2).
  * Training, inference, the resampling and the equilibrium initialisation
  * all run in the library's CUDA kernels on the network's device.
  * ====================================================================== */
@@ -285,6 +285,7 @@ typedef struct {
   int levels;               /* encoder levels, 1..6 */
   int device;
   unsigned long long seed;  /* weight initialisation */
+  int coords;               /* nonzero: three more input channels, the voxel's coordinates / R */
 } abx_net_params;
 
 typedef struct {

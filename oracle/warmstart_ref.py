@@ -89,8 +89,8 @@ def edt(solid: np.ndarray, sx: float, sy: float, sz: float) -> np.ndarray:
     return np.sqrt(best).reshape(R, R, R)
 
 
-def features(cls: np.ndarray, R: int, K: float):
-    """Network input (9, R, R, R) float32 and the exact wall distance (R, R, R) before scaling."""
+def features(cls: np.ndarray, R: int, K: float, coords: bool = False):
+    """Network input (9 or 12, R, R, R) float32 and the exact wall distance (R, R, R) before scaling."""
     nx, ny, nz = cls.shape
     n = _counts(nx, ny, nz, R)
     inv = np.float32(1.0) / n.astype(np.float32)
@@ -104,6 +104,13 @@ def features(cls: np.ndarray, R: int, K: float):
     x[4] = np.minimum(d / 20.0, 2.0).astype(np.float32)
     x[5] = np.float32(K) / np.float32(3.0)
     x[6], x[7], x[8] = np.float32(nx) / 128, np.float32(ny) / 64, np.float32(nz) / 128
+    if coords:
+        c = (np.arange(R, dtype=np.float32) + np.float32(0.5)) / np.float32(R)
+        xc = np.zeros((3, R, R, R), np.float32)
+        xc[0] = c[:, None, None]
+        xc[1] = c[None, :, None]
+        xc[2] = c[None, None, :]
+        x = np.concatenate([x, xc])
     return x, d
 
 
@@ -124,10 +131,10 @@ def targets(cls: np.ndarray, avg: dict, R: int, u0: float):
     return t, nf / n
 
 
-def conv_layers(base: int, levels: int):
+def conv_layers(base: int, levels: int, n_in: int = 9):
     """(cin, cout, stride, relu) of every convolution, in parameter order."""
     ch = [base << l for l in range(levels)]
-    out, c = [], 9
+    out, c = [], n_in
     for l in range(levels):
         out += [(c, ch[l], 1 if l == 0 else 2, True), (ch[l], ch[l], 1, True)]
         c = ch[l]
@@ -137,10 +144,10 @@ def conv_layers(base: int, levels: int):
     return out
 
 
-def unpack(weights: np.ndarray, base: int, levels: int, torch):
+def unpack(weights: np.ndarray, base: int, levels: int, torch, n_in: int = 9):
     """Per-layer (weight, bias) torch tensors (float64) from the flat parameter vector."""
     off, out = 0, []
-    for cin, cout, s, relu in conv_layers(base, levels):
+    for cin, cout, s, relu in conv_layers(base, levels, n_in):
         nw = cout * cin * 27
         w = torch.tensor(weights[off:off + nw].reshape(cout, cin, 3, 3, 3), dtype=torch.float64, requires_grad=True)
         b = torch.tensor(weights[off + nw:off + nw + cout], dtype=torch.float64, requires_grad=True)
@@ -151,7 +158,7 @@ def unpack(weights: np.ndarray, base: int, levels: int, torch):
 
 
 def net_forward(layers, x, levels: int, torch):
-    """The encoder-decoder of the warm start (x: (B, 9, R, R, R) float64)."""
+    """The encoder-decoder of the warm start (x: (B, 9 or 12, R, R, R) float64)."""
     F = torch.nn.functional
     it = iter(layers)
 

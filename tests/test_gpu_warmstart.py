@@ -34,15 +34,15 @@ def _torch():
     return torch
 
 
-@pytest.mark.parametrize("res,base,levels", [(8, 8, 2), (16, 8, 3)])
-def test_network_gradients_match_torch_autograd(res, base, levels):
+@pytest.mark.parametrize("res,base,levels,coords", [(8, 8, 2, False), (16, 8, 3, False), (8, 8, 2, True)])
+def test_network_gradients_match_torch_autograd(res, base, levels, coords):
     torch = _torch()
-    net = W.Net(res, base, levels, seed=3)
+    net = W.Net(res, base, levels, seed=3, coords=coords)
     w = net.get_weights()
-    assert w.size == net.n_params
+    assert w.size == net.n_params and net.info["in_channels"] == net.n_in
     rng = np.random.default_rng(1)
     B = 2
-    x = rng.standard_normal((B, 9, res, res, res)).astype(np.float32)
+    x = rng.standard_normal((B, net.n_in, res, res, res)).astype(np.float32)
     t = rng.standard_normal((B, 4, res, res, res)).astype(np.float32)
     m = rng.uniform(0, 1, (B, res, res, res)).astype(np.float32)
     scale = 1.0 / (4 * float(m.sum()))
@@ -54,7 +54,7 @@ def test_network_gradients_match_torch_autograd(res, base, levels):
                                 dgrad.data_ptr())
     pred, grad = dpred.cpu().numpy(), dgrad.cpu().numpy()
 
-    layers = R_.unpack(w, base, levels, torch)
+    layers = R_.unpack(w, base, levels, torch, net.n_in)
     X, T, M = (torch.tensor(a, dtype=torch.float64) for a in (x, t, m))
     P = R_.net_forward(layers, X, levels, torch)
     L = scale * (M[:, None] * (P - T) ** 2).sum()
@@ -72,9 +72,10 @@ def test_network_gradients_match_torch_autograd(res, base, levels):
     assert off == grad.size
 
 
-def test_features_and_targets_match_restatement():
+@pytest.mark.parametrize("coords", [False, True])
+def test_features_and_targets_match_restatement(coords):
     g = geometry()
-    net = W.Net(16, 8, 2)
+    net = W.Net(16, 8, 2, coords=coords)
     S = E.Simulation(g, RUN)
     S.run()
     net.add_sample(S)
@@ -82,8 +83,9 @@ def test_features_and_targets_match_restatement():
     fx, _ = net.predict(S)
     assert np.array_equal(x, fx)
     cls = R_.classes(g)
-    rx, dist = R_.features(cls, 16, RUN["K"])
-    for c in (0, 1, 2, 3, 5, 6, 7, 8):
+    rx, dist = R_.features(cls, 16, RUN["K"], coords)
+    assert x.shape[0] == rx.shape[0] == (12 if coords else 9)
+    for c in (0, 1, 2, 3, 5, 6, 7, 8) + ((9, 10, 11) if coords else ()):
         assert np.array_equal(x[c], rx[c]), f"feature channel {c}"
     assert (cls == 2).any() and (cls == 4).any()
     # jump flooding against the exact distance transform
