@@ -25,11 +25,14 @@
  * engine.js cannot run here (no JavaScript runtime).  STL parsing, the frame
  * transform, the parity voxelizer and the 27->1 downsample are pinned against
  * the reference's own Python CLI (airbox_cfd.py load_stl/to_local/voxelize),
- * imported and run to make tests/golden/.  The LBM step, probe and evaluate are
- * NOT pinned by any reference output ("parity unpinned" for those rows); they
- * are checked by known-answer properties (rest state, mass conservation, mirror
- * symmetry) and by the reference's own GPU-vs-CPU self-test criterion
- * (src/engine.js:597-611, threshold :772).
+ * imported and run to make tests/golden/, and so are the solid and fluid masks
+ * after downsample, duct, closing and flood, and the KPI formulas of evaluate
+ * (against the CLI's report() on its own averaged fields).  The LBM step and
+ * the probe are NOT pinned by any reference output ("parity unpinned" for those
+ * rows: the CLI's solver uses other boundary numerics); they are checked by
+ * known-answer properties (rest state, mass conservation, mirror symmetry) and
+ * by the reference's own GPU-vs-CPU self-test criterion (src/engine.js:597-611,
+ * threshold :772).
  */
 #include "engine_ref.h"
 

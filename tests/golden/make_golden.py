@@ -12,7 +12,11 @@ pin for the compute core:
   with the same jitter as src/engine.js:45-93;
 * ``main`` (airbox_cfd.py:143-223) run for one step - the 27->1 downsample
   (mean >= 0.25, i.e. at least 7 of 27), the inlet duct, the closed bottom and
-  the 6-connected flood from the inlet, saved as the solid and fluid masks.
+  the 6-connected flood from the inlet, saved as the solid and fluid masks;
+* ``report`` (airbox_cfd.py:296-314) - gamma, gamma core, the core shares under
+  50 % / over 150 %, reverse flow, peak-to-mean and zeta, computed by the CLI on
+  its own averaged fields of a 60-step run (fields and KPIs both stored), which
+  pins the formulas of evaluate() (src/engine.js:632-660).
 
 The JS path stores voxel hits as float32 and tests ``ceil(z/h - 0.5)``, the
 Python path keeps float64 and tests ``zc >= z``; the two agree unless a face
@@ -28,6 +32,7 @@ from __future__ import annotations
 import argparse
 import contextlib
 import io
+import json
 import math
 import os
 import sys
@@ -52,6 +57,11 @@ CASES = {
 }
 
 
+# report() result keys (airbox_cfd.py:360-363) in the order stored in the fixture
+REPORT_KPIS = ("gamma", "gamma_ohne_randzellen", "anteil_unter_50pct_kern", "anteil_ueber_150pct_kern",
+               "anteil_rueckstroemung", "max_zu_mittel", "zeta_rohluftseite")
+
+
 def _fake_matplotlib():
     mpl = types.ModuleType("matplotlib")
     mpl.use = lambda *a, **k: None
@@ -61,17 +71,22 @@ def _fake_matplotlib():
     return {"matplotlib": mpl, "matplotlib.pyplot": plt, "matplotlib.colors": colors}
 
 
-def run_main(R, stl_path, spec: ag.AirboxSpec, workdir):
-    argv = ["airbox_cfd.py", stl_path, "--dx", str(spec.dx), "--steps", "1", "--avg", "1",
+def run_main(R, stl_path, spec: ag.AirboxSpec, workdir, steps=1, avg=1):
+    """main() of the CLI; returns its saved fields and its report() KPIs (unrounded: the module's `round`
+    is replaced by the identity for the call)."""
+    argv = ["airbox_cfd.py", stl_path, "--dx", str(spec.dx), "--steps", str(steps), "--avg", str(avg),
             "--pleat", str(spec.pleat), "--tag", "g"]
     cwd = os.getcwd()
     os.chdir(workdir)
     try:
         with mock.patch.object(sys, "argv", argv), mock.patch.dict(sys.modules, _fake_matplotlib()), \
+                mock.patch.object(R, "round", lambda x, n=None: x, create=True), \
                 contextlib.redirect_stdout(io.StringIO()):
             R.main()
         d = np.load(os.path.join(workdir, "airbox_result_g.npz"))
-        return {k: d[k] for k in ("solid", "fluid")}
+        out = {k: d[k] for k in ("solid", "fluid", "ux", "uy", "uz", "rho")}
+        out["report"] = json.load(open(os.path.join(workdir, "airbox_ergebnis_g.json")))
+        return out
     finally:
         os.chdir(cwd)
 
@@ -127,6 +142,13 @@ def main():
             shape = tuple(int(math.ceil((mx[i] - origin[i] + h) / h)) for i in range(3))
             fine = R.voxelize(T, origin, tuple(s * 3 for s in shape), h / 3)
             masks = run_main(R, stl, spec, td)
+            if name == "small_baffle":
+                # report()'s KPIs (airbox_cfd.py:301-314) on the CLI's own averaged fields of a 60-step run
+                run = run_main(R, stl, spec, td, steps=60, avg=20)
+                for k in ("ux", "uy", "uz", "rho"):
+                    out[f"report_{name}_{k}"] = run[k].astype(np.float32)
+                rep = run["report"]
+                out[f"report_{name}_kpi"] = np.array([rep[k] for k in REPORT_KPIS], np.float64)
             out[f"vox_{name}_shape"] = np.array(fine.shape, np.int64)
             out[f"vox_{name}_fine"] = np.packbits(fine.ravel())
             out[f"vox_{name}_solid"] = np.packbits(masks["solid"].ravel())

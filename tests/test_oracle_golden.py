@@ -82,3 +82,24 @@ def test_voxelizer_and_masks_match_reference(name):
     n = int(np.prod(cshape))
     assert np.array_equal(g.solid(), np.unpackbits(GOLD[f"vox_{name}_solid"])[:n])
     assert np.array_equal(g.fluid(), np.unpackbits(GOLD[f"vox_{name}_fluid"])[:n])
+
+
+def test_evaluate_formulas_match_reference_report():
+    """report() of the reference's Python CLI (airbox_cfd.py:296-314) on its own averaged fields of a 60-step run
+    against the oracle's evaluate() (src/engine.js:632-660) on the same fields: the KPI formulas agree.  The CLI
+    sums float32 arrays with numpy's pairwise float32 sums where engine.js sums in float64, hence the tolerance."""
+    name = "small_baffle"
+    spec = ag.AirboxSpec(**SPECS[name])
+    g = O.prepare(ag.build_airbox(spec), spec.prepare_params())
+    S = O.OracleSim(g, dict(K=3.0, aniso=10.0, u=0.06, tau=0.51))
+    cells = S.cells()
+    acc = np.concatenate([GOLD[f"report_{name}_{k}"].ravel()[cells] for k in ("ux", "uy", "uz", "rho")])
+    m, _ = S.evaluate(acc.astype(np.float32))
+    ref = dict(zip(("gamma", "gammaCore", "lowCore", "highCore", "reverse", "maxToMean", "zeta"),
+                   GOLD[f"report_{name}_kpi"]))
+    for k in ("gamma", "gammaCore", "maxToMean", "zeta"):
+        assert abs(m[k] - ref[k]) <= 2e-5 * abs(ref[k]), (k, m[k], ref[k])
+    # shares of cells: counts over the core (cn cells) and the layer (n cells) agree to one cell
+    for k, n in (("lowCore", m["cn"]), ("highCore", m["cn"]), ("reverse", m["n"])):
+        assert abs(m[k] - ref[k]) * n <= 1 + 1e-9, (k, m[k], ref[k])
+    assert 0 < ref["lowCore"] < 1 and ref["zeta"] != 0
