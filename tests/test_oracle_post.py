@@ -104,3 +104,14 @@ def test_warmstart_features_of_a_synthetic_grid():
     n = R_._counts(20, 12, 18, 8)
     assert int(round(float((x[0].astype(np.float64) * n).sum()))) == int((cls > 0).sum())
     assert (d[x[0] < 0.5] == 0).all() and (d[x[0] >= 0.5] > 0).all()
+
+
+def test_warmstart_coordinate_channels():
+    cls = np.zeros((20, 12, 18), np.uint8)
+    cls[2:18, 2:10, 1:17] = 1
+    x, _ = R_.features(cls, 8, 3.0, coords=True)
+    assert x.shape == (12, 8, 8, 8)
+    c = (np.arange(8) + 0.5) / 8
+    assert np.allclose(x[9], c[:, None, None]) and np.allclose(x[10], c[None, :, None])
+    assert np.allclose(x[11], c[None, None, :])
+    assert [l[0] for l in R_.conv_layers(16, 4, 12)][0] == 12
