@@ -274,15 +274,34 @@ def _rel_err(m, ref):
             abs(m["zeta"] - ref["zeta"]) / abs(ref["zeta"]))
 
 
+def _feq_host(acc, NF):
+    """Equilibrium populations f[q*NF + a] (float32) of the averaged fields acc[c*NF + a] (cpuStep's feq)."""
+    import numpy as np
+    cx = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0])
+    cy = np.array([0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1])
+    cz = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1])
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    a = acc.reshape(4, NF).astype(np.float64)
+    ux, uy, uz, rho = a
+    u2 = ux * ux + uy * uy + uz * uz
+    f = np.empty((19, NF))
+    for q in range(19):
+        cu = cx[q] * ux + cy[q] * uy + cz[q] * uz
+        f[q] = w[q] * rho * (1 + 3 * cu + 4.5 * cu * cu - 1.5 * u2)
+    return f.astype(np.float32).ravel()
+
+
 def study_warmstart(seeds, weights: str, rules=WARM_RULES, uniform: bool = True, noise: bool = True,
-                    quiet: bool = False):
+                    perfect: bool = True, quiet: bool = False):
     """Time to converged gamma core / zeta: float16 storage + learned warm start + convergence run
     (abx_sim_solve_warm) against the plain float32 run on the reference's fixed schedule, on held-out
     seeded airboxes at dx 2 mm.  Wall times are host clocks around the solve (prepare excluded), each
     taken after one untimed solve of the same arm on the same simulation object (CUDA graphs built).
     With `uniform`, the same convergence run from f = w_i (float16) shows what the network adds.  With
     `noise`, the plain float32 run continued to 8000 steps (averaging 6000-8000) measures how far the
-    reference's own KPIs move between consecutive 2000-step windows: the noise floor of the +-1 % test."""
+    reference's own KPIs move between consecutive 2000-step windows: the noise floor of the +-1 % test.  With
+    `perfect`, the convergence run starts from the equilibrium of the plain run's own time-averaged field (what an
+    exact network would predict; the upload is not timed): the ceiling of the learned warm start."""
     from airboxcalc_gb300 import airboxgen as ag
     from airboxcalc_gb300 import engine as E
     from airboxcalc_gb300 import warmstart as W
@@ -305,6 +324,7 @@ def study_warmstart(seeds, weights: str, rules=WARM_RULES, uniform: bool = True,
             continue
         row = {"seed": seed, "K": K, "NF": P.NF, "plain_f32_ms": round(plain_ms, 2),
                "ref": {"gammaCore": ref["gammaCore"], "zeta": ref["zeta"]}}
+        f_perfect = _feq_host(P.get_acc(), P.NF) if perfect else None
         if noise:
             P.clear_acc()
             P.step(2000, True)
@@ -320,6 +340,19 @@ def study_warmstart(seeds, weights: str, rules=WARM_RULES, uniform: bool = True,
             row[f"warm{i}"] = {"ms": round(r["total_ms"], 2), "steps": r["steps"], "fell_back": r["fell_back"],
                                "infer_ms": round(r["infer_ms"], 3), "err_gammaCore": float(f"{eg:.3e}"),
                                "err_zeta": float(f"{ez:.3e}")}
+        if perfect:
+            for i, rule in enumerate(rules):
+                S.reset()
+                S.set_f(f_perfect)
+                W.converge(S, **rule)
+                S.reset()
+                S.set_f(f_perfect)
+                t0 = time.perf_counter()
+                r = W.converge(S, **rule)
+                ms = (time.perf_counter() - t0) * 1e3
+                eg, ez = _rel_err(r["metrics"], ref)
+                row[f"perfect{i}"] = {"ms": round(ms, 2), "steps": r["steps"], "converged": r["converged"],
+                                      "err_gammaCore": float(f"{eg:.3e}"), "err_zeta": float(f"{ez:.3e}")}
         if uniform:
             rule = rules[0]
             S.reset()
@@ -357,6 +390,9 @@ def study_warmstart(seeds, weights: str, rules=WARM_RULES, uniform: bool = True,
             "rules": [dict(r) for r in rules]}
     for i in range(len(rules)):
         summ[f"warm{i}_f16"] = summary(f"warm{i}")
+    if perfect:
+        for i in range(len(rules)):
+            summ[f"perfect{i}_f16"] = summary(f"perfect{i}")
     if uniform:
         summ["uniform0_f16"] = summary("uniform0")
     if noise:
@@ -576,6 +612,12 @@ def main():
     e2e_t = dist.max(sum(e2e_times)) / len(e2e_times)
     e2e = dist.sum(NF * run["steps"]) / e2e_t / 1e6
 
+    # the reference's whole evaluate() result object (cut planes, field3d, streamlines) on top of the KPIs
+    E.evaluate(S)
+    t0 = time.perf_counter()
+    E.evaluate(S)
+    evaluate_full_ms = (time.perf_counter() - t0) * 1e3
+
     # roofline of the fused step kernel (launches without averaging)
     bytes_per_cell = 2 * 19 * (4 if a.storage == "f32" else 2)
     avg_launch_ms = plain_ms / max(plain_launches, 1)
@@ -603,6 +645,7 @@ def main():
             "roofline": roofline,
             "gpu_launches": int(kernels),
             "gpu_launches_e2e_per_step": int(e2e_kernels),
+            "evaluate_full_result_ms": round(evaluate_full_ms, 2),
             "wall_s_timed": round(wall, 3),
             "clocks": clocks}
     if rank == 0 and not a.no_cpu_baseline:
@@ -614,7 +657,7 @@ def main():
         from airboxcalc_gb300 import warmstart as W
         if os.path.exists(W.WEIGHTS):
             summ, _ = study_warmstart(range(6000, 6012), W.WEIGHTS, rules=WARM_RULES[:1], uniform=False,
-                                      noise=False, quiet=True)
+                                      noise=False, perfect=False, quiet=True)
             w = summ["warm0_f16"]
             line["warm_start"] = {
                 "what": "time to converged gamma core / zeta: float16 + learned warm start + convergence run vs the "
