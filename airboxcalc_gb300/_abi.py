@@ -21,6 +21,8 @@ ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_OUT_OF_MEMORY = 20, 21, 22
 STORAGE = {"f32": 0, "f32exact": 1, "f16": 2, "bf16": 3, "f64": 4}
 
 # Every symbol include/airbox.h declares.
+ABI_VERSION = 2  # include/airbox.h ABX_ABI_VERSION: the structures below follow that version
+
 EXPORTS = [
     "abx_last_error", "abx_abi_version", "abx_device_count", "abx_parse_stl", "abx_prepare", "abx_geom_free",
     "abx_geom_get_info", "abx_geom_get_masks", "abx_geom_get_fine", "abx_sim_create", "abx_sim_free",
@@ -164,6 +166,8 @@ def load(build_if_missing: bool = True):
     if not os.path.exists(path):
         raise RuntimeError(f"{path} is missing: run airboxcalc_gb300.build.build() (needs nvcc)")
     L = C.CDLL(path)
+    if L.abx_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{path} implements ABI {L.abx_abi_version()}, these bindings ABI {ABI_VERSION}: rebuild it")
     vp = C.c_void_p
     L.abx_last_error.restype = C.c_char_p
     L.abx_parse_stl.argtypes = [C.c_char_p, C.c_size_t, vp, C.c_size_t, C.POINTER(C.c_size_t)]

@@ -23,7 +23,9 @@
 extern "C" {
 #endif
 
-#define ABX_ABI_VERSION 1
+/* Version of the structures and entry points below; a host compares it with abx_abi_version() before use.
+ * 2: prepare timings in abx_geom_info, coordinate channels in abx_net_params, batch groups. */
+#define ABX_ABI_VERSION 2
 
 /* Status codes.  The first group mirrors the errors engine.js throws. */
 typedef enum {
