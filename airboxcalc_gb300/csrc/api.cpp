@@ -671,6 +671,8 @@ static StepArgs step_args(const abx_sim &s) {
   a.acc = s.d_acc; a.ns = s.has_ns ? s.d_ns : nullptr; a.status = s.d_status; a.diag = s.d_diag;
   offsets(*s.g, a.off);
   a.u0 = s.u0; a.tau0 = s.tau0; a.sig = s.sig; a.aniso = s.aniso; a.cs2s = s.cs2s;
+  a.u0f = (float)s.u0; a.tau0f = (float)s.tau0; a.sigf = (float)s.sig; a.anisof = (float)s.aniso;
+  a.cs2sf = (float)s.cs2s;
   return a;
 }
 static StateArgs state_args(const abx_sim &s) {

@@ -20,6 +20,9 @@ struct StepArgs {
   unsigned long long *diag;  // 8 words: where a pipeline wait gave up (TMA kernel), or null
   long long off[19];       // pull offset of direction q in the padded layout
   double u0, tau0, sig, aniso, cs2s;
+  // the same five rounded to float32 on the host: the float32 collision reads them straight from the
+  // parameter bank instead of converting the doubles in every warp (a slow pipe on this GPU)
+  float u0f, tau0f, sigf, anisof, cs2sf;
 };
 
 struct StateArgs {
@@ -94,6 +97,7 @@ struct BatchParams {
   StepArgs v[kBatchChunk];
   uint32_t vbase;
 };
+static_assert(sizeof(BatchParams) <= 32764, "kernel parameter limit");
 constexpr int kBatchShapes = 3;
 int batch_shape_spw(int shape);
 int batch_shape_minblocks(int shape);

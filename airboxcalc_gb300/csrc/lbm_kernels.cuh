@@ -33,7 +33,11 @@ namespace abx {
 
 template <class L> __device__ __forceinline__ CollideParams<L> make_params(const StepArgs &a) {
   CollideParams<L> P;
-  P.u0 = (L)a.u0; P.tau0 = (L)a.tau0; P.sig = (L)a.sig; P.aniso = (L)a.aniso; P.cs2s = (L)a.cs2s;
+  if constexpr (sizeof(L) == 4) {
+    P.u0 = a.u0f; P.tau0 = a.tau0f; P.sig = a.sigf; P.aniso = a.anisof; P.cs2s = a.cs2sf;
+  } else {
+    P.u0 = (L)a.u0; P.tau0 = (L)a.tau0; P.sig = (L)a.sig; P.aniso = (L)a.aniso; P.cs2s = (L)a.cs2s;
+  }
   return P;
 }
 
