@@ -22,6 +22,7 @@ STORAGE = {"f32": 0, "f32exact": 1, "f16": 2, "bf16": 3, "f64": 4}
 
 # Every symbol include/airbox.h declares.
 ABI_VERSION = 2  # include/airbox.h ABX_ABI_VERSION: the structures below follow that version
+MAX_LINE_POINTS = 2001  # include/airbox.h ABX_MAX_LINE_POINTS
 
 EXPORTS = [
     "abx_last_error", "abx_abi_version", "abx_device_count", "abx_parse_stl", "abx_prepare", "abx_geom_free",

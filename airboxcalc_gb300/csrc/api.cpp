@@ -421,6 +421,7 @@ static int build_device_geometry(abx_geom &g, cudaStream_t st) {
   CK(cudaMalloc((void **)&g.d_seg, sizeof(uint2) * std::max<unsigned long long>(nseg, 1)), "prepare: segments");
   CK(prep_segments(a, W, (const uint32_t *)dbits.p, g.nzp, g.kpad, g.d_seg, (uint32_t *)dbc2.p,
                    (unsigned long long *)doff2.p, st), "prepare: segments");
+  CK(prep_seg_interior(g.d_seg, g.nseg, g.d_mask, st), "prepare: segments");
   // the air of layers jm and top+1 in compact order (the progress probe's cells, :327-333)
   auto layer = [&](int j, std::vector<int64_t> &out) -> int {
     out.clear();
@@ -437,7 +438,7 @@ static int build_device_geometry(abx_geom &g, cudaStream_t st) {
   };
   if (int rc = layer(g.jm, g.layer_m)) return rc;
   if (int rc = layer(g.top + 1, g.layer_t)) return rc;
-  g.launches += 9;
+  g.launches += 10;
   g.h2d += ny;
   g.d2h += (int64_t)(sizeof kc + 3 * sizeof(unsigned long long));
   return ABX_OK;

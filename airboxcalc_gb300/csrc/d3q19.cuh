@@ -30,6 +30,12 @@ __host__ __device__ constexpr int wclass(int q) { return q == 0 ? 0 : (q <= 6 ? 
 constexpr uint32_t kFluidBit = 1u;
 constexpr int kClassShift = 19;
 constexpr uint32_t kClsBulk = 0, kClsInlet = 1, kClsOutlet = 2, kClsFilter = 3;
+// mask word of a bulk cell whose 18 pull neighbours are all fluid
+constexpr uint32_t kMaskInterior = 0x7FFFFu;
+// Segment entry {base | flag, lane mask}: bit 31 of the base marks a segment whose fluid cells all have the
+// mask word kMaskInterior (the step kernels then skip the mask load).  Bases stay below 2^31 (19 Np < 2^32).
+constexpr uint32_t kSegInterior = 0x80000000u;
+__host__ __device__ __forceinline__ uint32_t seg_base(uint2 s) { return s.x & ~kSegInterior; }
 
 // Storage formats of the populations.  Shifted formats hold f - w_q.
 enum StoreKind { kStoreF32 = 0, kStoreF32Exact = 1, kStoreF16 = 2, kStoreBF16 = 3, kStoreF64 = 4 };

@@ -6,6 +6,8 @@
 #include <vector_types.h>
 #include <stdint.h>
 
+#include "airbox.h"
+
 namespace abx {
 
 struct StepArgs {
@@ -171,6 +173,8 @@ cudaError_t prep_cells(const MaskArgs &a, int64_t nzp, int64_t kpad, int64_t *ce
                        unsigned long long *offsets, cudaStream_t st);
 cudaError_t prep_segments(const MaskArgs &a, int W, const uint32_t *bits, int64_t nzp, int64_t kpad, uint2 *seg,
                           uint32_t *block_counts, unsigned long long *offsets, cudaStream_t st);
+// set the interior flag (kSegInterior) of the segments whose fluid cells all carry the mask word kMaskInterior
+cudaError_t prep_seg_interior(uint2 *seg, uint32_t nseg, const uint32_t *mask, cudaStream_t st);
 
 // ---------------------------------------------------------------- post-processing (postproc.cu)
 struct PostArgs {
@@ -185,7 +189,7 @@ struct PostArgs {
   double u0;
   const float *avg;          // [4][Np] averages as float32 (post_average), read by the kernels below
 };
-constexpr int kMaxLinePoints = 2001;   // points one streamline can keep (6000 steps, every 3rd, plus the last)
+constexpr int kMaxLinePoints = ABX_MAX_LINE_POINTS;   // points one streamline can keep (6000 steps, every 3rd, plus the last)
 // the float32 averages sum / nacc of every padded cell into avg (4 * Np floats)
 cudaError_t post_average(const PostArgs &a, float *avg, cudaStream_t st);
 // field3d: d_scal receives pin and rhoRef; spd/pst/loss (nx*ny*nz floats, may be null)

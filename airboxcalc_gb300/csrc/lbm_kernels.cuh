@@ -78,8 +78,10 @@ __device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, cons
   for (int j = 0; j < SPW; j++) {
     act[j] = (sg[j].y >> lane) & 1u;
     // 32-bit element indices: the host guarantees 19 * Np < 2^32
-    p[j] = sg[j].x + lane;
-    m[j] = act[j] ? a.mask[p[j]] : 0u;  // in flight together with the population loads below
+    p[j] = seg_base(sg[j]) + lane;
+    // in flight together with the population loads below; known without a load in the interior segments of
+    // an odd step (even steps keep the plain load: their 16-bit kernels have no register to spare for the branch)
+    m[j] = act[j] ? ((ODD && (sg[j].x & kSegInterior)) ? kMaskInterior : a.mask[p[j]]) : 0u;
     if (!act[j]) continue;
     if (ODD) {
       // Pull from the neighbours first.  For a fluid cell x every x - c_q lies
@@ -102,7 +104,7 @@ __device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, cons
 #pragma unroll
   for (int j = 0; j < SPW; j++) {
     if (!act[j]) continue;
-    if (ODD && m[j] != 0x7FFFFu) {
+    if (ODD && m[j] != kMaskInterior) {
 #pragma unroll
       for (int q = 1; q < 19; q++)
         if (!((m[j] >> q) & 1u)) fi[j][q] = S::ldr(f + ((uint32_t)q * Np + p[j]));
@@ -114,13 +116,19 @@ __device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, cons
     if constexpr (sizeof(L) == 4)
       collide_fast<HAS_NS, S::kShifted>(fi[j], cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
     else collide<L, HAS_NS>(fi[j], cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
+    if (ODD && (sg[j].x & kSegInterior)) {
+      // every neighbour is fluid: each population goes to the neighbour's slot (warp-uniform branch)
 #pragma unroll
-    for (int q = 0; q < 19; q++) {
-      uint32_t idx;
-      if (ODD)
-        idx = ((m[j] >> opp(q)) & 1u) ? (uint32_t)q * Np + p[j] + (uint32_t)a.off[q] : (uint32_t)opp(q) * Np + p[j];
-      else idx = (uint32_t)opp(q) * Np + p[j];
-      S::str(f + idx, fo[q]);
+      for (int q = 0; q < 19; q++) S::str(f + ((uint32_t)q * Np + p[j] + (uint32_t)a.off[q]), fo[q]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 19; q++) {
+        uint32_t idx;
+        if (ODD)
+          idx = ((m[j] >> opp(q)) & 1u) ? (uint32_t)q * Np + p[j] + (uint32_t)a.off[q] : (uint32_t)opp(q) * Np + p[j];
+        else idx = (uint32_t)opp(q) * Np + p[j];
+        S::str(f + idx, fo[q]);
+      }
     }
     if (ACC) {
       Acc *acc = (Acc *)a.acc;

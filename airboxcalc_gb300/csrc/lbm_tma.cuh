@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2)
     const uint32_t t = blockIdx.x + i * G0;
     if (t >= ntiles) break;
     const uint32_t s0 = t * kTmaSegs + warp;
-    ABX_ISSUE(t, i, (s0 < nseg ? seg[s0] : make_uint2(0, 0)));
+    ABX_ISSUE(t, i, (s0 < nseg ? make_uint2(seg_base(seg[s0]), seg[s0].y) : make_uint2(0, 0)));
   }
   __syncthreads();   // the segment table of the first stages is visible to every lane
 
@@ -247,7 +247,8 @@ __global__ void __launch_bounds__(kTmaThreads, 2)
     // next use of this stage: tile n + STAGES; its segment entry is loaded now, used after the compute
     const uint32_t tn = blockIdx.x + (n + STAGES) * G0;
     const uint32_t sn = tn * kTmaSegs + warp;
-    const uint2 sg_next = (tn < ntiles && sn < nseg) ? seg[sn] : make_uint2(0, 0);
+    uint2 sg_next = (tn < ntiles && sn < nseg) ? seg[sn] : make_uint2(0, 0);
+    sg_next.x = seg_base(sg_next);   // this kernel stages every segment's mask words
     const bool ok = mbar_wait(bar, parity);
     if (ok && threadIdx.x == 0 && tn < ntiles)
       mbar_expect_tx(bar, min((uint32_t)kTmaSegs, nseg - tn * kTmaSegs) * ST::kSegBytes);

@@ -230,11 +230,15 @@ cudaError_t post_planes(const PostArgs &a, int ic, int jc, int jlow, float *out,
   return cudaGetLastError();
 }
 
+// Seeds per block of the streamline kernel.
+#ifndef ABX_TRACE_TPB
+#define ABX_TRACE_TPB 32
+#endif
 cudaError_t post_streamlines(const PostArgs &a, const double *seeds, int nseeds, int top, double *pts, int *count,
                              cudaStream_t st) {
   if (nseeds <= 0) return cudaSuccess;
-  const unsigned blocks = (unsigned)((nseeds + 31) / 32);
-  streamline_kernel<<<blocks, 32, 0, st>>>(a, seeds, nseeds, top, pts, count);
+  const unsigned blocks = (unsigned)((nseeds + ABX_TRACE_TPB - 1) / ABX_TRACE_TPB);
+  streamline_kernel<<<blocks, ABX_TRACE_TPB, 0, st>>>(a, seeds, nseeds, top, pts, count);
   return cudaGetLastError();
 }
 

@@ -20,6 +20,7 @@
 // Integer work only; every result is independent of scheduling.
 #include <stdint.h>
 
+#include "d3q19.cuh"
 #include "lbm_iface.h"
 
 namespace abx {
@@ -350,6 +351,26 @@ cudaError_t prep_cells(const MaskArgs &a, int64_t nzp, int64_t kpad, int64_t *ce
                        unsigned long long *offsets, cudaStream_t st) {
   const CellItems it{a.fluid, a.nz, nzp, kpad};
   return compact(it, a.N, cells, block_counts, offsets, st);
+}
+
+// One warp per segment: flag the segment interior when every fluid lane's mask word is kMaskInterior.
+__global__ void seg_interior_kernel(uint2 *seg, uint32_t nseg, const uint32_t *__restrict__ mask) {
+  const uint32_t s = blockIdx.x * 8u + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
+  if (s >= nseg) return;   // uniform per warp
+  const uint2 g = seg[s];
+  const bool edge = ((g.y >> lane) & 1u) && mask[seg_base(g) + lane] != kMaskInterior;
+  const unsigned any = __ballot_sync(0xffffffffu, edge);
+  if (lane == 0 && !any) seg[s].x = seg_base(g) | kSegInterior;
+}
+
+// ABX_SEG_INTERIOR=0 leaves every segment unflagged (every step loads every mask word)
+#ifndef ABX_SEG_INTERIOR
+#define ABX_SEG_INTERIOR 1
+#endif
+cudaError_t prep_seg_interior(uint2 *seg, uint32_t nseg, const uint32_t *mask, cudaStream_t st) {
+  if (nseg == 0 || !ABX_SEG_INTERIOR) return cudaSuccess;
+  seg_interior_kernel<<<(nseg + 7u) / 8u, 256, 0, st>>>(seg, nseg, mask);
+  return cudaGetLastError();
 }
 
 cudaError_t prep_segments(const MaskArgs &a, int W, const uint32_t *bits, int64_t nzp, int64_t kpad, uint2 *seg,

@@ -298,16 +298,14 @@ class Simulation:
     def streamlines(self, maxSeeds: int = 220) -> dict:
         """streamlines (src/engine.js:721-758), traced on the GPU: pts (model coordinates), spd, off."""
         i = A.LinesInfo()
-        L = A.load()
-        rc = L.abx_sim_streamlines(self._h, maxSeeds, None, None, None, 0, 0, C.byref(i))
-        if rc not in (A.OK, A.ERR_INVALID_ARGUMENT):
-            _check(rc)
-        pts = np.empty(3 * max(i.n_points, 1), np.float32)
-        spd = np.empty(max(i.n_points, 1), np.float32)
-        off = np.empty(i.n_lines + 1, np.uint32)
-        _check(L.abx_sim_streamlines(self._h, maxSeeds, _ptr(pts), _ptr(spd), _ptr(off), i.n_points,
-                                     i.n_lines + 1, C.byref(i)))
-        return {"pts": pts[:3 * i.n_points], "spd": spd[:i.n_points], "off": off}
+        # capacities that always suffice: one call traces once
+        cap = (maxSeeds + 1) * A.MAX_LINE_POINTS
+        pts = np.empty(3 * cap, np.float32)
+        spd = np.empty(cap, np.float32)
+        off = np.empty(maxSeeds + 2, np.uint32)
+        _check(A.load().abx_sim_streamlines(self._h, maxSeeds, _ptr(pts), _ptr(spd), _ptr(off), cap, maxSeeds + 2,
+                                            C.byref(i)))
+        return {"pts": pts[:3 * i.n_points], "spd": spd[:i.n_points], "off": off[:i.n_lines + 1]}
 
     def set_timing(self, on: bool = True):
         _check(A.load().abx_sim_set_timing(self._h, 1 if on else 0))

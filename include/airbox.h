@@ -205,7 +205,11 @@ int abx_sim_planes(abx_sim *s, float *out, abx_planes_info *info);
 /* streamlines (src/engine.js:721-758) traced on the device, one thread per
  * seed: pts (3 floats per point, model coordinates), spd (|u|/u0 per point),
  * off (n_lines + 1 prefix counts).  With capacities too small (e.g. 0) the
- * counts are still reported and ABX_ERR_INVALID_ARGUMENT is returned. */
+ * counts are still reported and ABX_ERR_INVALID_ARGUMENT is returned.  A line
+ * keeps at most ABX_MAX_LINE_POINTS points and at most max_seeds + 1 seeds are
+ * traced, so cap_points = (max_seeds + 1) * ABX_MAX_LINE_POINTS and
+ * cap_lines = max_seeds + 2 always suffice (one call, one trace). */
+#define ABX_MAX_LINE_POINTS 2001
 typedef struct {
   int seeds_opening, seeds_traced, n_lines, n_points;
 } abx_lines_info;
