@@ -5,7 +5,7 @@
 //                loss on the whole grid (NaN where there is no air)
 //   planes       src/engine.js:662-680: the cut planes planInlet, planLow, lon
 //   streamlines  src/engine.js:721-758: RK2 traces of the averaged velocity from
-//                the inlet opening, one thread per seed
+//                the inlet opening, one warp per seed
 //
 // The averages are read as the reference holds them: the Float32Array of
 // simulate() (sum / nacc rounded to float32, :356), made once per call.  Sums the reference takes
@@ -147,26 +147,93 @@ __global__ void planes_kernel(const PostArgs a, int ic, int jc, int jlow, float 
   }
 }
 
-__device__ double trace_vel(const PostArgs &a, const AvgView &U, double x, double y, double z, double out[3]) {
+// The streamline trace on the GB300's float64 units: their throughput is a small fraction of float32's, and
+// one thread per seed makes each RK2 step a long chain of dependent float64 instructions.  Here one warp traces
+// one seed and the independent parts of each step run on separate lanes: the eight trilinear corners (lanes
+// 0..7), the four running sums over the corners (lanes 0..3: x, y, z velocity and the weights, each added in
+// the reference's corner order), and the per-axis divisions (lanes 0..2).  Every lane holds the same position,
+// so the trace's branches are warp-uniform; every value is the reference's float64 operation sequence.
+struct TraceWarp {
+  double (*cor)[4];   // [8][4] this warp's corner products (w u_x, w u_y, w u_z, w), shared memory
+  double *bc;         // [4] broadcast slots, shared memory
+  int lane;
+};
+
+// Sum of w * u over the air corners of (x, y, z) (the trilinear loop of :741-747) into v[0..2], the weight sum
+// returned.
+__device__ double trace_vel_warp(const PostArgs &a, const AvgView &U, const TraceWarp &t, double x, double y, double z,
+                                 double v[3]) {
   const double fi0 = floor(x), fj0 = floor(y), fk0 = floor(z);
   const double fx = x - fi0, fy = y - fj0, fz = z - fk0;
   const int i0 = (int)fi0, j0 = (int)fj0, k0 = (int)fk0;
-  out[0] = out[1] = out[2] = 0;
-  double wsum = 0;
-  for (int da = 0; da < 2; da++)
-    for (int db = 0; db < 2; db++)
-      for (int dc = 0; dc < 2; dc++) {
-        const int i = i0 + da, j = j0 + db, k = k0 + dc;
-        if (i < 0 || j < 0 || k < 0 || i >= a.nx || j >= a.ny || k >= a.nz) continue;
+  bool valid = false;
+  if (t.lane < 8) {
+    // corner lane = da * 4 + db * 2 + dc: the reference loop's nesting order
+    const int da = (t.lane >> 2) & 1, db = (t.lane >> 1) & 1, dc = t.lane & 1;
+    const int i = i0 + da, j = j0 + db, k = k0 + dc;
+    if (!(i < 0 || j < 0 || k < 0 || i >= a.nx || j >= a.ny || k >= a.nz)) {
+      const int64_t p = padded(a, i, j, k);
+      if (air(a, p)) {
         const double w = (da ? fx : 1 - fx) * (db ? fy : 1 - fy) * (dc ? fz : 1 - fz);
-        const int64_t p = padded(a, i, j, k);
-        if (!air(a, p)) continue;
-        out[0] += w * U(0, p);
-        out[1] += w * U(1, p);
-        out[2] += w * U(2, p);
-        wsum += w;
+        t.cor[t.lane][0] = w * U(0, p);
+        t.cor[t.lane][1] = w * U(1, p);
+        t.cor[t.lane][2] = w * U(2, p);
+        t.cor[t.lane][3] = w;
+        valid = true;
       }
+    }
+  }
+  const unsigned vm = __ballot_sync(0xffffffffu, valid);
+  __syncwarp();
+  if (t.lane < 4) {
+    double s = 0;
+    for (int l = 0; l < 8; l++)
+      if ((vm >> l) & 1u) s += t.cor[l][t.lane];
+    t.bc[t.lane] = s;
+  }
+  __syncwarp();
+  v[0] = t.bc[0]; v[1] = t.bc[1]; v[2] = t.bc[2];
+  const double wsum = t.bc[3];
+  __syncwarp();   // the slots are rewritten by the next call
   return wsum;
+}
+
+// Math.hypot (V8: scale by the largest magnitude, Kahan-compensated sum of squares), the three scalings on
+// lanes 0..2
+__device__ double js_hypot3_warp(const TraceWarp &t, double x, double y, double z) {
+  const double a[3] = {fabs(x), fabs(y), fabs(z)};
+  for (int i = 0; i < 3; i++) if (isinf(a[i])) return INFINITY;
+  double mx = 0;
+  for (int i = 0; i < 3; i++) {
+    if (isnan(a[i])) return NAN;
+    if (a[i] > mx) mx = a[i];
+  }
+  if (mx == 0) return 0;
+  if (t.lane < 3) t.bc[t.lane] = (t.lane == 0 ? a[0] : t.lane == 1 ? a[1] : a[2]) / mx;
+  __syncwarp();
+  const double n3[3] = {t.bc[0], t.bc[1], t.bc[2]};
+  __syncwarp();
+  double sum = 0, comp = 0;
+  for (int i = 0; i < 3; i++) {
+    const double summand = n3[i] * n3[i] - comp;
+    const double pre = sum + summand;
+    comp = (pre - sum) - summand;
+    sum = pre;
+  }
+  return sqrt(sum) * mx;
+}
+
+// base[c] + (f * v[c]) / m for c = 0, 1, 2 (lane c), left to right as the reference writes it
+__device__ void trace_step_warp(const TraceWarp &t, const double base[3], double f, const double v[3], double m,
+                                double out[3]) {
+  if (t.lane < 3) {
+    const double b = t.lane == 0 ? base[0] : t.lane == 1 ? base[1] : base[2];
+    const double c = t.lane == 0 ? v[0] : t.lane == 1 ? v[1] : v[2];
+    t.bc[t.lane] = b + f * c / m;
+  }
+  __syncwarp();
+  out[0] = t.bc[0]; out[1] = t.bc[1]; out[2] = t.bc[2];
+  __syncwarp();
 }
 
 __device__ __forceinline__ bool trace_inside(const PostArgs &a, double x, double y, double z) {
@@ -175,32 +242,43 @@ __device__ __forceinline__ bool trace_inside(const PostArgs &a, double x, double
   return air(a, padded(a, (int)ri, (int)rj, (int)rk));
 }
 
-// One thread per seed: the trace of :739-751, up to kMaxLinePoints points (x, y, z, |u|/u0) in
-// grid-cell coordinates into the seed's slot; count[s] = points kept.
-__global__ void streamline_kernel(const PostArgs a, const double *seeds, int nseeds, int top, double *pts,
-                                  int *count) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nseeds) return;
+constexpr int kTraceWarps = 4;   // seeds per block
+
+// One warp per seed: the trace of :739-751, up to kMaxLinePoints points (x, y, z, |u|/u0) in grid-cell
+// coordinates into the seed's slot; count[s] = points kept.
+__global__ void __launch_bounds__(32 * kTraceWarps) streamline_kernel(const PostArgs a, const double *seeds, int nseeds,
+                                                                      int top, double *pts, int *count) {
+  __shared__ double cor[kTraceWarps][8][4];
+  __shared__ double bc[kTraceWarps][4];
+  const int wib = threadIdx.x >> 5;
+  const int s = blockIdx.x * kTraceWarps + wib;
+  if (s >= nseeds) return;   // whole warps leave together
+  const TraceWarp t{cor[wib], bc[wib], (int)(threadIdx.x & 31)};
   const AvgView U{a.avg, a.Np};
-  double x = seeds[3 * s], y = seeds[3 * s + 1], z = seeds[3 * s + 2], v1[3], v2[3];
+  double pos[3] = {seeds[3 * s], seeds[3 * s + 1], seeds[3 * s + 2]}, mid[3], v1[3], v2[3];
   double *P = pts + (int64_t)s * 4 * kMaxLinePoints;
   const double ds = 0.35;
   int m = 0;
   for (int st = 0; st < 6000; st++) {
-    if (!trace_inside(a, x, y, z) || trace_vel(a, U, x, y, z, v1) < 0.3) break;
-    const double m1 = js_hypot3(v1[0], v1[1], v1[2]);
+    if (!trace_inside(a, pos[0], pos[1], pos[2]) || trace_vel_warp(a, U, t, pos[0], pos[1], pos[2], v1) < 0.3) break;
+    const double m1 = js_hypot3_warp(t, v1[0], v1[1], v1[2]);
     if (m1 < 0.01 * a.u0) break;
-    if (st % 3 == 0) { P[4 * m] = x; P[4 * m + 1] = y; P[4 * m + 2] = z; P[4 * m + 3] = m1 / a.u0; m++; }
-    const double xm = x + 0.5 * ds * v1[0] / m1, ym = y + 0.5 * ds * v1[1] / m1, zm = z + 0.5 * ds * v1[2] / m1;
-    if (trace_vel(a, U, xm, ym, zm, v2) < 0.3) break;
-    const double m2 = js_hypot3(v2[0], v2[1], v2[2]);
+    if (st % 3 == 0) {
+      if (t.lane == 0) { P[4 * m] = pos[0]; P[4 * m + 1] = pos[1]; P[4 * m + 2] = pos[2]; P[4 * m + 3] = m1 / a.u0; }
+      m++;
+    }
+    trace_step_warp(t, pos, 0.5 * ds, v1, m1, mid);
+    if (trace_vel_warp(a, U, t, mid[0], mid[1], mid[2], v2) < 0.3) break;
+    const double m2 = js_hypot3_warp(t, v2[0], v2[1], v2[2]);
     if (m2 < 0.01 * a.u0) break;
-    x += ds * v2[0] / m2;
-    y += ds * v2[1] / m2;
-    z += ds * v2[2] / m2;
-    if (y < top + 0.5) { P[4 * m] = x; P[4 * m + 1] = y; P[4 * m + 2] = z; P[4 * m + 3] = m2 / a.u0; m++; break; }
+    trace_step_warp(t, pos, ds, v2, m2, pos);
+    if (pos[1] < top + 0.5) {
+      if (t.lane == 0) { P[4 * m] = pos[0]; P[4 * m + 1] = pos[1]; P[4 * m + 2] = pos[2]; P[4 * m + 3] = m2 / a.u0; }
+      m++;
+      break;
+    }
   }
-  count[s] = m;
+  if (t.lane == 0) count[s] = m;
 }
 
 static unsigned grid_of(int64_t n) {
@@ -230,15 +308,11 @@ cudaError_t post_planes(const PostArgs &a, int ic, int jc, int jlow, float *out,
   return cudaGetLastError();
 }
 
-// Seeds per block of the streamline kernel.
-#ifndef ABX_TRACE_TPB
-#define ABX_TRACE_TPB 32
-#endif
 cudaError_t post_streamlines(const PostArgs &a, const double *seeds, int nseeds, int top, double *pts, int *count,
                              cudaStream_t st) {
   if (nseeds <= 0) return cudaSuccess;
-  const unsigned blocks = (unsigned)((nseeds + ABX_TRACE_TPB - 1) / ABX_TRACE_TPB);
-  streamline_kernel<<<blocks, ABX_TRACE_TPB, 0, st>>>(a, seeds, nseeds, top, pts, count);
+  const unsigned blocks = (unsigned)((nseeds + kTraceWarps - 1) / kTraceWarps);
+  streamline_kernel<<<blocks, 32 * kTraceWarps, 0, st>>>(a, seeds, nseeds, top, pts, count);
   return cudaGetLastError();
 }
 

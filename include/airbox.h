@@ -202,7 +202,7 @@ typedef struct {
 } abx_planes_info;
 int abx_sim_planes(abx_sim *s, float *out, abx_planes_info *info);
 
-/* streamlines (src/engine.js:721-758) traced on the device, one thread per
+/* streamlines (src/engine.js:721-758) traced on the device, one warp per
  * seed: pts (3 floats per point, model coordinates), spd (|u|/u0 per point),
  * off (n_lines + 1 prefix counts).  With capacities too small (e.g. 0) the
  * counts are still reported and ABX_ERR_INVALID_ARGUMENT is returned.  A line
