@@ -213,6 +213,33 @@ __device__ __forceinline__ void collide(const L (&fi)[19], uint32_t cls, L nsv, 
   }
 }
 
+// Reciprocal and square root of collide_fast: correctly rounded, or (FAST) the hardware approximations
+// (rcp.approx / sqrt.approx: about one unit in the last place, one MUFU instruction instead of an iteration
+// with a special-case branch).  The 16-bit storages take FAST (ABX_FAST_MATH16, default 1): their kernels are
+// short of issue slots and their stored values carry 11 or 8 significant bits (config2 float16 step 38.8 ->
+// 37.0 us); the float32 kernels keep the correctly rounded forms (no gain there: config3 1038 vs 1049 us).
+#ifndef ABX_FAST_MATH16
+#define ABX_FAST_MATH16 1
+#endif
+template <bool FAST> __device__ __forceinline__ float cf_rcp(float x) {
+  if constexpr (FAST) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+  } else {
+    return 1.0f / x;
+  }
+}
+template <bool FAST> __device__ __forceinline__ float cf_sqrt(float x) {
+  if constexpr (FAST) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+  } else {
+    return sqrtf(x);
+  }
+}
+
 // The same collision in float32 with the algebra rearranged for the GPU:
 // moments and the stress tensor from the nine opposite-pair sums s and
 // differences d (f_q +- f_opp(q)), the non-equilibrium stress as
@@ -245,7 +272,8 @@ __device__ __forceinline__ void collide_fast(const float (&f)[19], uint32_t cls,
   const float jx = d1 + (d7 + d9) + (d11 + d13);
   const float jy = d3 + (d7 - d9) + (d15 + d17);
   const float jz = d5 + (d11 - d13) + (d15 - d17);
-  const float inv = 1.0f / rho;
+  constexpr bool FAST = SHIFTED && ABX_FAST_MATH16;
+  const float inv = cf_rcp<FAST>(rho);
   ux = jx * inv; uy = jy * inv; uz = jz * inv;
   float vx = ux, vy = uy, vz = uz;   // velocity of the equilibrium
   float r = rho, omega = 1.0f;       // omega = 1: equilibrium overwrite (inlet/outlet)
@@ -266,14 +294,14 @@ __device__ __forceinline__ void collide_fast(const float (&f)[19], uint32_t cls,
     const float nxz = (s11 - s13) - jx * uz;
     const float nyz = (s15 - s17) - jy * uz;
     const float q2 = nxx * nxx + nyy * nyy + nzz * nzz + 2.0f * (nxy * nxy + nxz * nxz + nyz * nyz);
-    const float tau = 0.5f * (P.tau0 + sqrtf(P.tau0 * P.tau0 + P.cs2s * sqrtf(q2) * inv));
+    const float tau = 0.5f * (P.tau0 + cf_sqrt<FAST>(P.tau0 * P.tau0 + P.cs2s * cf_sqrt<FAST>(q2) * inv));
     if (cls == kClsFilter) {
       const float a1 = tau * P.sig * P.aniso, a2 = tau * P.sig;
       const float sl = 1.0f - (a1 >= 0.9f ? 0.9f : a1), sv = 1.0f - (a2 >= 0.9f ? 0.9f : a2);  // Math.min, NaN kept
       vx = ux * sl; vy = uy * sv; vz = uz * sl;
       ux = 0.5f * (ux + vx); uy = 0.5f * (uy + vy); uz = 0.5f * (uz + vz);
     }
-    omega = 1.0f / tau;
+    omega = cf_rcp<FAST>(tau);
   }
   const float base = 1.0f - 1.5f * (vx * vx + vy * vy + vz * vz);
   const float w1 = r * (1.0f / 18.0f), w2 = r * (1.0f / 36.0f);
