@@ -172,3 +172,52 @@ def test_net_argument_errors():
         net.add_sample(S)          # no averages yet
     with pytest.raises(E.AirboxError):
         net.train(0, 1, 1)         # no samples
+
+
+# D3Q19 velocities in the library's population order (src/engine.js:4-12).
+CX = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0])
+CY = np.array([0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1])
+CZ = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1])
+
+
+def test_trained_network_beats_the_uniform_start():
+    """What the shipped, trained network gains over the same method without it, on held-out airboxes
+    (seeds 6000-6011 of the generator at dx 2 mm; training used seeds 0-1999):
+
+    * its start is much closer to the plain float32 run's time-averaged velocity than the uniform start
+      f = w_i, whose velocity is zero (relative L2 error exactly 1);
+    * the same float16 convergence run (default stop rule) ends with smaller gamma core / zeta errors
+      against the plain float32 run on the reference's 6000/2000 schedule when it starts from the network's
+      prediction (abx_sim_solve_warm) than when it starts from f = w_i (abx_sim_converge after a reset).
+    """
+    net = W.Net.load()
+    start_err, warm_err, uniform_err = [], [], []
+    for seed in range(6000, 6012):
+        spec, K = W.variant(seed)
+        run = dict(W.RUN, K=K)
+        try:
+            g = E.prepare({"tris": ag.build_airbox(spec), **spec.prepare_params(), "maxCells": 1e10})
+            P = E.Simulation(g, run)
+            P.run()
+        except E.AirboxError:        # leaking or unstable draws have no reference result
+            continue
+        ref = P.evaluate()["metrics"]
+        ubar = P.get_acc().reshape(4, P.NF)[:3].astype(np.float64)
+        del P
+        S = E.Simulation(g, dict(run, storage="f16"))
+        W.warm_start(S, net)
+        f = S.get_f().reshape(19, S.NF).astype(np.float64)
+        u0 = np.stack([CX @ f, CY @ f, CZ @ f]) / f.sum(0)
+        start_err.append(np.linalg.norm(u0 - ubar) / np.linalg.norm(ubar))
+
+        def err(m):
+            return max(abs(m[k] - ref[k]) / abs(ref[k]) for k in ("gammaCore", "zeta"))
+
+        warm_err.append(err(W.solve_warm(S, net)["metrics"]))
+        S.reset()
+        uniform_err.append(err(W.converge(S)["metrics"]))
+        del S, g
+    assert len(warm_err) >= 6, "too few stable held-out airboxes"
+    assert np.median(start_err) < 0.6, start_err
+    assert np.median(warm_err) < np.median(uniform_err), (warm_err, uniform_err)
+    assert sum(e < 0.01 for e in warm_err) >= sum(e < 0.01 for e in uniform_err), (warm_err, uniform_err)
