@@ -144,7 +144,7 @@ struct abx_geom {
   double h = 0, hf = 0, origin[3] = {0, 0, 0}, mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0}, pleat = 0;
   bool has_outlet = false;
   std::vector<float> tris_local, xc, dc, zc;
-  std::vector<uint8_t> opening;      // nx*ny (host: the opening search runs on the host)
+  std::vector<uint8_t> opening;      // nx*ny, host copy of d_opening
   // device-side, shared by the simulations of this geometry
   uint8_t *d_solid = nullptr, *d_fluid = nullptr, *d_outlet = nullptr;   // N bytes each
   uint32_t *d_mask = nullptr;
@@ -181,86 +181,134 @@ struct DevBuf {  // scoped device allocation
   void *p = nullptr;
   ~DevBuf() { if (p) cudaFree(p); }
 };
+struct AsyncBuf {  // scoped stream-ordered allocation (cudaMallocAsync), freed on its stream
+  void *p = nullptr;
+  cudaStream_t st = nullptr;
+  ~AsyncBuf() { if (p) cudaFreeAsync(p, st); }
+};
 struct StreamHolder {
   cudaStream_t s = nullptr;
   ~StreamHolder() { if (s) cudaStreamDestroy(s); }
 };
 }  // namespace
 
-// Opening search, duct, closing, flood, leak check and outlet (src/engine.js:141-216) on the host.
-static int finish_geometry(abx_geom &g, const abx_prepare_params *p, const std::vector<uint8_t> &slice,
-                           cudaStream_t st) {
-  const int nx = g.nx, ny = g.ny, nz = g.nz, nxf = g.nxf, nyf = g.nyf;
-  const double h = g.h, hf = g.hf;
+// Opening search on the fine slice (src/engine.js:141-171), on the GPU: g.d_opening (device), g.opening (host
+// copy), g.nHoles, g.nOpen; the reference's errors when no hole is large enough or the opening is too small.
+static int find_opening(abx_geom &g, const abx_prepare_params *p, const uint8_t *d_slice, cudaStream_t st) {
+  const int nx = g.nx, ny = g.ny, nxf = g.nxf, nyf = g.nyf;
   const int64_t nfs = (int64_t)nxf * nyf;
-  // holes: empty fine cells of slice kf not 4-connected to the border, below the seal (:142-154)
-  std::vector<uint8_t> outside(nfs, 0);
-  std::vector<int32_t> q(nfs);
-  int64_t qh = 0, qt = 0;
-  auto push = [&](int64_t c) { if (!slice[c] && !outside[c]) { outside[c] = 1; q[qt++] = (int32_t)c; } };
-  for (int i = 0; i < nxf; i++) { push((int64_t)i * nyf); push((int64_t)i * nyf + nyf - 1); }
-  for (int j = 0; j < nyf; j++) { push(j); push((int64_t)(nxf - 1) * nyf + j); }
-  while (qh < qt) {
-    const int64_t c = q[qh++];
-    const int i = (int)(c / nyf), j = (int)(c % nyf);
-    if (i > 0) push(c - nyf);
-    if (i < nxf - 1) push(c + nyf);
-    if (j > 0) push(c - 1);
-    if (j < nyf - 1) push(c + 1);
-  }
-  std::vector<uint8_t> holes(nfs);
-  for (int64_t c = 0; c < nfs; c++)
-    holes[c] = !slice[c] && !outside[c] && (g.origin[1] + ((double)(c % nyf) + 0.5) * hf > 0) ? 1 : 0;
-  // components2d (:95-108): labelled in scan order, cells in BFS order
-  std::vector<int32_t> lab(nfs, -1), cells;
-  cells.reserve(1024);
-  std::vector<std::pair<int64_t, int64_t>> comps;  // (start, length) in `cells`
-  for (int64_t s = 0; s < nfs; s++) {
-    if (!holes[s] || lab[s] >= 0) continue;
-    const int id = (int)comps.size();
-    const int64_t start = (int64_t)cells.size();
-    cells.push_back((int32_t)s);
-    lab[s] = id;
-    for (int64_t head = start; head < (int64_t)cells.size(); head++) {
-      const int64_t c = cells[head];
-      const int i = (int)(c / nyf), j = (int)(c % nyf);
-      const int64_t nb[4] = {i > 0 ? c - nyf : -1, i < nxf - 1 ? c + nyf : -1, j > 0 ? c - 1 : -1,
-                             j < nyf - 1 ? c + 1 : -1};
-      for (int64_t d : nb)
-        if (d >= 0 && holes[d] && lab[d] < 0) { lab[d] = id; cells.push_back((int32_t)d); }
+  // a kept component has more than 25 / hf^2 cells
+  const double kcap = std::floor((double)nfs * g.hf * g.hf / 25.0) + 2;
+  const uint32_t cap = (uint32_t)std::min<double>(kcap, (double)nfs + 1);
+  // one stream-ordered scratch block: outside, labels, sizes, claims, result, flag, kept list, coarse counters
+  auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+  size_t nb = 0;
+  const size_t o_out = nb;  nb += al(sizeof(OpenOut));
+  const size_t o_flag = nb; nb += al(sizeof(int));
+  const size_t o_lab = nb;  nb += al(sizeof(int32_t) * (size_t)nfs);
+  const size_t o_size = nb; nb += al(sizeof(uint32_t) * (size_t)nfs);
+  const size_t o_clm = nb;  nb += al(sizeof(uint32_t) * (size_t)nfs);
+  const size_t o_kept = nb; nb += al(sizeof(uint2) * cap);
+  const size_t o_sel = nb;  nb += al(sizeof(uint32_t) * (size_t)nx * ny);
+  const size_t o_outs = nb; nb += al((size_t)nfs);
+  AsyncBuf scratch{nullptr, st};
+  CK(cudaMallocAsync(&scratch.p, nb, st), "prepare: opening");
+  unsigned char *S = (unsigned char *)scratch.p;
+  OpenArgs a{d_slice, nxf, nyf, S + o_outs, (int32_t *)(S + o_lab), (uint32_t *)(S + o_size),
+             (uint32_t *)(S + o_clm), g.origin[0], g.origin[1], g.hf};
+  OpenOut *out = (OpenOut *)(S + o_out);
+  int *changed = (int *)(S + o_flag);
+  uint2 *kept = (uint2 *)(S + o_kept);
+  CK(cudaMemsetAsync(out, 0, sizeof(OpenOut), st), "prepare: opening");
+  CK(open_init(a, st), "prepare: opening");
+  g.launches += 1;
+  // empty cells reachable from the border (:144-151), then the holes' components (:153-155, components2d
+  // :95-108): rounds of line sweeps until a round changes nothing (each round changes a cell otherwise)
+  for (int pass = 0; pass < 2; pass++) {
+    if (pass == 1) {
+      CK(open_holes(a, st), "prepare: opening");
+      g.launches += 1;
     }
-    comps.emplace_back(start, (int64_t)cells.size() - start);
+    for (int64_t round = 0;; round++) {
+      if (round > nfs) return fail(ABX_ERR_CUDA, "prepare: opening search did not settle");
+      CK(cudaMemsetAsync(changed, 0, sizeof(int), st), "prepare: opening");
+      CK(pass == 0 ? open_outside_round(a, changed, st) : open_label_round(a, changed, st), "prepare: opening");
+      int c = 0;
+      CK(cudaMemcpyAsync(&c, changed, sizeof(int), cudaMemcpyDeviceToHost, st), "prepare: opening");
+      CK(cudaStreamSynchronize(st), "prepare: opening");
+      g.launches += 3;
+      g.d2h += sizeof(int);
+      if (!c) break;
+    }
   }
-  std::vector<std::pair<int64_t, int64_t>> keep;
-  for (auto &c : comps)
-    if ((double)c.second * hf * hf > 25) keep.push_back(c);
-  g.nHoles = (int)keep.size();
-  if (keep.empty()) return fail(ABX_ERR_NO_OPENING, "Auf der gewählten Einlassseite wurde keine Öffnung gefunden.");
-  size_t best = 0;
+  CK(open_components(a, out, kept, cap, st), "prepare: opening");
+  OpenOut o{};
+  CK(cudaMemcpyAsync(&o, out, sizeof o, cudaMemcpyDeviceToHost, st), "prepare: opening");
+  CK(cudaStreamSynchronize(st), "prepare: opening");
+  g.launches += 2;
+  g.d2h += sizeof o;
+  if (o.n_kept > cap) return fail(ABX_ERR_CUDA, "prepare: more openings than the search holds");
+  g.nHoles = (int)o.n_kept;
+  if (!o.n_kept) return fail(ABX_ERR_NO_OPENING, "Auf der gewählten Einlassseite wurde keine Öffnung gefunden.");
+  uint32_t root = 0xFFFFFFFFu - (uint32_t)(o.best & 0xFFFFFFFFull);   // the largest, first of equals (:168)
   if (p->has_click) {
+    // the component holding the sampled cell nearest to the click, first of equals in component order (:158-163)
+    const int n = (int)o.n_kept;
+    std::vector<uint2> kv(n);
+    CK(cudaMemcpyAsync(kv.data(), kept, sizeof(uint2) * n, cudaMemcpyDeviceToHost, st), "prepare: opening");
+    CK(cudaStreamSynchronize(st), "prepare: opening");
+    std::vector<int64_t> offs(n);
+    int64_t tot = 0;
+    for (int b = 0; b < n; b++) { offs[b] = tot; tot += kv[b].y; }
+    // per component: its cells in breadth-first order, its offset in that array, its smallest distance
+    const size_t b_off = al(sizeof(int32_t) * (size_t)std::max<int64_t>(tot, 1)), b_min = b_off + al(sizeof(int64_t) * n);
+    AsyncBuf bfs{nullptr, st};
+    CK(cudaMallocAsync(&bfs.p, b_min + sizeof(unsigned long long) * n, st), "prepare: opening");
+    unsigned char *B = (unsigned char *)bfs.p;
+    CK(cudaMemcpyAsync(B + b_off, offs.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, st), "prepare: opening");
     double L[3];
     g.fr.local(p->click, L);
+    CK(open_bfs_click(a, kept, (const int64_t *)(B + b_off), n, (int32_t *)B, L[0], L[1],
+                      (unsigned long long *)(B + b_min), st), "prepare: opening");
+    std::vector<unsigned long long> dm(n);
+    CK(cudaMemcpyAsync(dm.data(), B + b_min, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, st),
+       "prepare: opening");
+    CK(cudaStreamSynchronize(st), "prepare: opening");
+    g.launches += 1;
+    g.h2d += (int64_t)(sizeof(int64_t) * n);
+    g.d2h += (int64_t)((sizeof(uint2) + sizeof(unsigned long long)) * n);
+    std::vector<int> idx(n);
+    for (int b = 0; b < n; b++) idx[b] = b;
+    std::sort(idx.begin(), idx.end(), [&](int x, int y) { return kv[x].x < kv[y].x; });
     double bd = INFINITY;
-    for (size_t ci = 0; ci < keep.size(); ci++)
-      for (int64_t s = 0; s < keep[ci].second; s += 3) {
-        const int32_t c = cells[keep[ci].first + s];
-        const double x = g.origin[0] + ((double)(c / nyf) + 0.5) * hf, y = g.origin[1] + ((double)(c % nyf) + 0.5) * hf;
-        const double d = (x - L[0]) * (x - L[0]) + (y - L[1]) * (y - L[1]);
-        if (d < bd) { bd = d; best = ci; }
-      }
-  } else {
-    for (size_t ci = 1; ci < keep.size(); ci++)
-      if (keep[ci].second > keep[best].second) best = ci;
+    for (int b : idx) {
+      double d;
+      std::memcpy(&d, &dm[b], sizeof d);
+      if (d < bd) { bd = d; root = kv[b].x; }
+    }
   }
-  std::vector<uint8_t> sel((size_t)nx * ny, 0);
-  for (int64_t s = 0; s < keep[best].second; s++) {
-    const int32_t c = cells[keep[best].first + s];
-    sel[(size_t)((c / nyf) / 3) * ny + ((c % nyf) / 3)]++;
-  }
+  // coarse opening: cells holding at least 5 of their 9 fine cells in the chosen component (:164-166)
+  uint32_t *sel = (uint32_t *)(S + o_sel);
+  CK(cudaMemsetAsync(sel, 0, sizeof(uint32_t) * (size_t)nx * ny, st), "prepare: opening");
+  CK(cudaMalloc((void **)&g.d_opening, std::max<size_t>((size_t)nx * ny, 1)), "prepare: opening");
+  CK(open_select(a, root, nx, ny, sel, g.d_opening, out, st), "prepare: opening");
   g.opening.assign((size_t)nx * ny, 0);
-  g.nOpen = 0;
-  for (size_t c = 0; c < sel.size(); c++) if (sel[c] >= 5) { g.opening[c] = 1; g.nOpen++; }
+  CK(cudaMemcpyAsync(g.opening.data(), g.d_opening, g.opening.size(), cudaMemcpyDeviceToHost, st), "prepare: opening");
+  CK(cudaMemcpyAsync(&o, out, sizeof o, cudaMemcpyDeviceToHost, st), "prepare: opening");
+  CK(cudaStreamSynchronize(st), "prepare: opening");
+  g.launches += 2;
+  g.d2h += (int64_t)(g.opening.size() + sizeof o);
+  g.nOpen = (int)o.n_open;
   if (g.nOpen < 8) return fail(ABX_ERR_OPENING_TOO_SMALL, "Einlassöffnung ist zu klein für die gewählte Zellgröße.");
+  return ABX_OK;
+}
+
+// Opening search (GPU), then duct, closing, flood, leak check and outlet (src/engine.js:141-216).
+static int finish_geometry(abx_geom &g, const abx_prepare_params *p, const uint8_t *d_slice, cudaStream_t st) {
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  const double h = g.h;
+  int rc = find_opening(g, p, d_slice, st);
+  if (rc) return rc;
 
   // device: inlet duct, closed bottom, flood, leak, outlet (:174-216)
   g.kw0 = -1;
@@ -271,8 +319,6 @@ static int finish_geometry(abx_geom &g, const abx_prepare_params *p, const std::
   for (int j = 0; j < ny; j++) if ((double)g.dc[j] >= 0) { g.top = j; break; }
   if (g.top < 0) return fail(ABX_ERR_SEAL_OUTSIDE, "Dichtebene liegt außerhalb des Modells.");
   const int top = g.top;
-  CK(cudaMalloc((void **)&g.d_opening, std::max<size_t>(g.opening.size(), 1)), "prepare: opening");
-  CK(cudaMemcpyAsync(g.d_opening, g.opening.data(), g.opening.size(), cudaMemcpyHostToDevice, st), "prepare: opening");
   DevBuf dclose, dflag, dcount;
   CK(cudaMalloc(&dclose.p, ny), "prepare: rows");
   CK(cudaMemcpyAsync(dclose.p, close_row.data(), ny, cudaMemcpyHostToDevice, st), "prepare: rows");
@@ -283,7 +329,7 @@ static int finish_geometry(abx_geom &g, const abx_prepare_params *p, const std::
   MaskArgs a{nx, ny, nz, g.N, g.d_solid, g.d_fluid, g.d_outlet, g.d_opening, (const uint8_t *)dclose.p, g.kw0, top};
   CK(prep_duct(a, st), "prepare: duct");
   g.launches += 2;
-  g.h2d += (int64_t)(g.opening.size() + ny);
+  g.h2d += (int64_t)ny;
   // flood: rounds of line sweeps until a round adds no cell (each round at least one cell otherwise)
   int *changed = (int *)dflag.p;
   for (int64_t round = 0;; round++) {
@@ -522,16 +568,14 @@ extern "C" int abx_prepare(const float *tris, size_t nfloats, const abx_prepare_
   VoxJob job{(const float *)dtris.p, ntri, {g.origin[0], g.origin[1], g.origin[2]}, hf, g.nx, g.ny, g.nz, g.kf};
   VoxOut vo{(uint8_t *)dsolid.p, (uint8_t *)dslice.p, nullptr};
   CK(run_voxelizer(job, vo, sh.s), "prepare: voxelize");
-  std::vector<uint8_t> slice((size_t)g.nxf * g.nyf);
-  CK(cudaMemcpyAsync(slice.data(), dslice.p, slice.size(), cudaMemcpyDeviceToHost, sh.s), "prepare: download");
   CK(cudaStreamSynchronize(sh.s), "prepare: sync");
   g.d_solid = (uint8_t *)dsolid.p;   // the geometry keeps the solid mask on the device
   dsolid.p = nullptr;
   g.launches += vo.launches;
   g.h2d += (int64_t)(sizeof(float) * nfloats);
-  g.d2h += vo.d2h_bytes + (int64_t)slice.size();
+  g.d2h += vo.d2h_bytes;
   const auto t1 = clk::now();
-  int rc = finish_geometry(g, p, slice, sh.s);
+  int rc = finish_geometry(g, p, (const uint8_t *)dslice.p, sh.s);
   if (rc) return rc;
   const auto t2 = clk::now();
   rc = build_device_geometry(g, sh.s);

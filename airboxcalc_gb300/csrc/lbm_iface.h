@@ -176,6 +176,41 @@ cudaError_t prep_segments(const MaskArgs &a, int W, const uint32_t *bits, int64_
 // set the interior flag (kSegInterior) of the segments whose fluid cells all carry the mask word kMaskInterior
 cudaError_t prep_seg_interior(uint2 *seg, uint32_t nseg, const uint32_t *mask, cudaStream_t st);
 
+// Opening search on the fine slice kf (src/engine.js:141-171), prepare.cu.  Cell c = i*nyf + j.
+struct OpenArgs {
+  const uint8_t *slice;    // nxf*nyf: 1 where the fine voxel (i, j, kf) is material
+  int nxf, nyf;
+  uint8_t *outside;        // empty cells 4-connected to the slice's border
+  int32_t *label;          // hole cells: the lowest index of their component (its root); -1 elsewhere
+  uint32_t *size;          // at a root: the cells of its component
+  uint32_t *claim;         // breadth-first search of the click case
+  double origin0, origin1, hf;
+};
+struct OpenOut {
+  unsigned long long best;   // (size << 32) | (0xFFFFFFFF - root) of the largest kept component (first of equals)
+  uint32_t n_kept;           // components above 25 mm^2
+  uint32_t n_open;           // coarse opening cells
+};
+// outside seeded on the border, labels and sizes cleared, claims freed
+cudaError_t open_init(const OpenArgs &a, cudaStream_t st);
+// one round of line sweeps along j and i; *changed |= 1 when a cell joined the outside
+cudaError_t open_outside_round(const OpenArgs &a, int *changed, cudaStream_t st);
+// holes (empty, not outside, cell centre below the seal) labelled with their own index
+cudaError_t open_holes(const OpenArgs &a, cudaStream_t st);
+// one round of line sweeps carrying the lowest label along runs of hole cells
+cudaError_t open_label_round(const OpenArgs &a, int *changed, cudaStream_t st);
+// component sizes, then the kept components ({root, size} into kept, at most cap) and out->best / n_kept
+cudaError_t open_components(const OpenArgs &a, OpenOut *out, uint2 *kept, uint32_t cap, cudaStream_t st);
+// click: for each of the n kept components, the reference's breadth-first order of its cells (into order at
+// offs[b]) and the smallest squared distance to (cx, cy) over every third cell of that order (bits of the
+// double, into dmin[b])
+cudaError_t open_bfs_click(const OpenArgs &a, const uint2 *kept, const int64_t *offs, int n, int32_t *order,
+                           double cx, double cy, unsigned long long *dmin, cudaStream_t st);
+// the coarse opening: cells (nx*ny) holding at least 5 of their 9 fine cells in the component of `root`;
+// sel (nx*ny counters) must be zero; out->n_open += opening cells
+cudaError_t open_select(const OpenArgs &a, uint32_t root, int nx, int ny, uint32_t *sel, uint8_t *opening,
+                        OpenOut *out, cudaStream_t st);
+
 // ---------------------------------------------------------------- post-processing (postproc.cu)
 struct PostArgs {
   int nx, ny, nz;

@@ -1,6 +1,14 @@
 // prepare.cu - the mask stages of prepare() and the device geometry of
 // setupSim on the GPU.
 //
+//   opening          src/engine.js:141-171 on the fine slice kf: empty cells
+//                    4-connected to the slice border (line sweeps to a fixed
+//                    point), holes below the seal, their 4-connected components
+//                    (label = lowest index, i.e. the reference's scan-order
+//                    numbering), sizes, the components above 25 mm^2, the
+//                    largest (first of equals) or, with a click, the one whose
+//                    every-third cell in the reference's breadth-first order
+//                    comes closest, and the coarse cells holding 5 of 9
 //   duct / closing   src/engine.js:174-178: cells before the inlet wall are
 //                    solid except under the opening; rows beyond the model's
 //                    depth are solid
@@ -17,7 +25,8 @@
 //                    runs with their lane masks, and the compact cell list
 //                    (cells in (i, j, k) order, the reference's compact order)
 //
-// Integer work only; every result is independent of scheduling.
+// Integer work (and float64 with explicitly rounded operations where the
+// reference compares coordinates); every result is independent of scheduling.
 #include <stdint.h>
 
 #include "d3q19.cuh"
@@ -53,6 +62,11 @@ __global__ void seed_kernel(const MaskArgs a) {
   }
 }
 
+// Lines are walked in chunks of kWalk cells whose loads are issued together before the chunk is processed in
+// order (a line's cells ahead of the walk are written only by the walking thread itself): along j and i the
+// steps are nz and ny*nz cells apart, and one dependent load per step would wait on the memory latency.
+constexpr int kWalk = 16;
+
 // One sweep along AXIS (2: k, 1: j, 0: i), one thread per grid line, forward then backward: a cell joins
 // the air when its predecessor on the line is air and it is open (not solid, j >= top).
 template <int AXIS>
@@ -70,21 +84,26 @@ __global__ void sweep_kernel(const MaskArgs a, int *changed) {
     else if (AXIS == 1) { base = (l / a.nz) * a.ny * a.nz + l % a.nz; }
     else { base = l; jfix = (int)(l / a.nz); }
     if (jfix >= 0 && jfix < a.top) continue;   // the whole line is closed
-    uint8_t prev = a.fluid[base];
-    for (int t = 1; t < len; t++) {
-      const int64_t c = base + t * stride;
-      uint8_t f = a.fluid[c];
-      const bool open = !a.solid[c] && (AXIS == 1 ? t >= a.top : true);
-      if (!f && prev && open) { a.fluid[c] = 1; f = 1; any = true; }
-      prev = f;
-    }
-    prev = a.fluid[base + (int64_t)(len - 1) * stride];
-    for (int t = len - 2; t >= 0; t--) {
-      const int64_t c = base + t * stride;
-      uint8_t f = a.fluid[c];
-      const bool open = !a.solid[c] && (AXIS == 1 ? t >= a.top : true);
-      if (!f && prev && open) { a.fluid[c] = 1; f = 1; any = true; }
-      prev = f;
+    for (int dir = 0; dir < 2; dir++) {
+      // forward: t = 1 .. len-1 after t = 0; backward: t = len-2 .. 0 after t = len-1
+      uint8_t prev = a.fluid[base + (dir ? (int64_t)(len - 1) * stride : 0)];
+      for (int s0 = 1; s0 < len; s0 += kWalk) {
+        uint8_t f[kWalk], sol[kWalk];
+#pragma unroll
+        for (int u = 0; u < kWalk; u++) {
+          const int s = s0 + u, t = dir ? len - 1 - s : s;
+          if (s < len) { f[u] = a.fluid[base + t * stride]; sol[u] = a.solid[base + t * stride]; }
+        }
+#pragma unroll
+        for (int u = 0; u < kWalk; u++) {
+          const int s = s0 + u, t = dir ? len - 1 - s : s;
+          if (s < len) {
+            const bool open = !sol[u] && (AXIS == 1 ? t >= a.top : true);
+            if (!f[u] && prev && open) { a.fluid[base + t * stride] = 1; f[u] = 1; any = true; }
+            prev = f[u];
+          }
+        }
+      }
     }
   }
   if (__syncthreads_or(any) && threadIdx.x == 0) atomicOr(changed, 1);
@@ -378,6 +397,284 @@ cudaError_t prep_segments(const MaskArgs &a, int W, const uint32_t *bits, int64_
   const int S = (int)(nzp / 32);
   const SegItems it{bits, W, S, nzp, kpad};
   return compact(it, (int64_t)a.nx * a.ny * S, seg, block_counts, offsets, st);
+}
+
+// ------------------------------------------------------------------ opening search (src/engine.js:141-171)
+constexpr uint32_t kClaimFree = 0xFFFFFFFFu, kClaimDone = 0xFFFFFFFEu;
+
+__global__ void open_init_kernel(const OpenArgs a) {
+  const int64_t n = (int64_t)a.nxf * a.nyf;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c / a.nyf), j = (int)(c % a.nyf);
+    const bool border = i == 0 || i == a.nxf - 1 || j == 0 || j == a.nyf - 1;
+    a.outside[c] = (border && !a.slice[c]) ? 1 : 0;
+    a.label[c] = -1;
+    a.size[c] = 0;
+    a.claim[c] = kClaimFree;
+  }
+}
+
+// ROWS: one thread per row i, along j; else one thread per column j, along i (a row apart per step), walked
+// in chunks of kWalk cells.  Forward then backward: an empty cell joins the outside when its predecessor on
+// the line is outside.
+template <bool ROWS>
+__global__ void open_outside_kernel(const OpenArgs a, int *changed) {
+  const int lines = ROWS ? a.nxf : a.nyf, len = ROWS ? a.nyf : a.nxf;
+  const int64_t stride = ROWS ? 1 : a.nyf;
+  bool any = false;
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < lines; l += gridDim.x * blockDim.x) {
+    const int64_t base = ROWS ? (int64_t)l * a.nyf : (int64_t)l;
+    for (int dir = 0; dir < 2; dir++) {
+      // forward: t = 1 .. len-1 after t = 0; backward: t = len-2 .. 0 after t = len-1
+      uint8_t prev = a.outside[base + (dir ? (int64_t)(len - 1) * stride : 0)];
+      for (int s0 = 1; s0 < len; s0 += kWalk) {
+        uint8_t o[kWalk], m[kWalk];
+#pragma unroll
+        for (int u = 0; u < kWalk; u++) {
+          const int s = s0 + u, t = dir ? len - 1 - s : s;
+          if (s < len) { o[u] = a.outside[base + t * stride]; m[u] = a.slice[base + t * stride]; }
+        }
+#pragma unroll
+        for (int u = 0; u < kWalk; u++) {
+          const int s = s0 + u, t = dir ? len - 1 - s : s;
+          if (s < len) {
+            if (!o[u] && prev && !m[u]) { a.outside[base + t * stride] = 1; o[u] = 1; any = true; }
+            prev = o[u];
+          }
+        }
+      }
+    }
+  }
+  if (__syncthreads_or(any) && threadIdx.x == 0) atomicOr(changed, 1);
+}
+
+// holes (:153): empty, not outside, fine-cell centre below the seal (origin_1 + (j + 0.5) hf > 0)
+__global__ void open_holes_kernel(const OpenArgs a) {
+  const int64_t n = (int64_t)a.nxf * a.nyf;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(c % a.nyf);
+    const double y = __dadd_rn(a.origin1, __dmul_rn((double)j + 0.5, a.hf));
+    a.label[c] = (!a.slice[c] && !a.outside[c] && y > 0.0) ? (int32_t)c : -1;
+  }
+}
+
+// the lower label moves along runs of hole cells, forward then backward (walked in chunks like the outside);
+// at the fixed point every cell of a component carries the component's lowest index
+template <bool ROWS>
+__global__ void open_label_kernel(const OpenArgs a, int *changed) {
+  const int lines = ROWS ? a.nxf : a.nyf, len = ROWS ? a.nyf : a.nxf;
+  const int64_t stride = ROWS ? 1 : a.nyf;
+  bool any = false;
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < lines; l += gridDim.x * blockDim.x) {
+    const int64_t base = ROWS ? (int64_t)l * a.nyf : (int64_t)l;
+    for (int dir = 0; dir < 2; dir++) {
+      int32_t prev = a.label[base + (dir ? (int64_t)(len - 1) * stride : 0)];
+      for (int s0 = 1; s0 < len; s0 += kWalk) {
+        int32_t v[kWalk];
+#pragma unroll
+        for (int u = 0; u < kWalk; u++) {
+          const int s = s0 + u, t = dir ? len - 1 - s : s;
+          if (s < len) v[u] = a.label[base + t * stride];
+        }
+#pragma unroll
+        for (int u = 0; u < kWalk; u++) {
+          const int s = s0 + u, t = dir ? len - 1 - s : s;
+          if (s < len) {
+            if (v[u] >= 0 && prev >= 0 && prev < v[u]) { a.label[base + t * stride] = prev; v[u] = prev; any = true; }
+            prev = v[u];
+          }
+        }
+      }
+    }
+  }
+  if (__syncthreads_or(any) && threadIdx.x == 0) atomicOr(changed, 1);
+}
+
+__global__ void open_size_kernel(const OpenArgs a) {
+  const int64_t n = (int64_t)a.nxf * a.nyf;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t l = a.label[c];
+    if (l >= 0) atomicAdd(a.size + l, 1u);
+  }
+}
+
+// kept components (:155): cells * hf * hf > 25, in the reference's left-to-right float64 order
+__global__ void open_roots_kernel(const OpenArgs a, OpenOut *out, uint2 *kept, uint32_t cap) {
+  const int64_t n = (int64_t)a.nxf * a.nyf;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    if (a.label[c] != (int32_t)c) continue;
+    const uint32_t s = a.size[c];
+    if (!(__dmul_rn(__dmul_rn((double)s, a.hf), a.hf) > 25.0)) continue;
+    const uint32_t k = atomicAdd(&out->n_kept, 1u);
+    if (k < cap) kept[k] = make_uint2((uint32_t)c, s);
+    atomicMax(&out->best, ((unsigned long long)s << 32) | (0xFFFFFFFFull - (unsigned long long)c));
+  }
+}
+
+// neighbour `slot` of cell c in components2d's order (:102): i-1, i+1, j-1, j+1; -1 outside the slice
+__device__ __forceinline__ int32_t open_nb(const OpenArgs &a, int32_t c, int slot) {
+  const int i = c / a.nyf, j = c % a.nyf;
+  switch (slot) {
+    case 0: return i > 0 ? c - a.nyf : -1;
+    case 1: return i < a.nxf - 1 ? c + a.nyf : -1;
+    case 2: return j > 0 ? c - 1 : -1;
+    default: return j < a.nyf - 1 ? c + 1 : -1;
+  }
+}
+
+// squared distance of fine cell c's centre to the click, as in :160-161 (rounded operations, no fusion), as
+// the bits of the (non-negative) double: ordered like the values
+__device__ __forceinline__ unsigned long long open_dist_bits(const OpenArgs &a, int32_t c, double cx, double cy) {
+  const double x = __dadd_rn(a.origin0, __dmul_rn((double)(c / a.nyf) + 0.5, a.hf));
+  const double y = __dadd_rn(a.origin1, __dmul_rn((double)(c % a.nyf) + 0.5, a.hf));
+  const double dx = __dsub_rn(x, cx), dy = __dsub_rn(y, cy);
+  return (unsigned long long)__double_as_longlong(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+}
+
+// One block per kept component: its breadth-first order, level by level.  The queue of components2d
+// (:99-104) appends, for each cell in queue order, its unvisited neighbours in slot order; so a cell of the
+// next level is appended by the first cell of the current level (in queue order) that has it as a
+// neighbour, and its place in the next level is the rank of (parent's place * 4 + slot) among all such
+// claims.  Pass 1 takes the smallest claim per cell (atomicMin), pass 2 ranks the winning claims with a
+// block-wide scan in claim order.
+constexpr int kBfsThreads = 1024;
+__global__ void __launch_bounds__(kBfsThreads) open_bfs_kernel(const OpenArgs a, const uint2 *kept,
+                                                               const int64_t *offs, int32_t *order, double cx,
+                                                               double cy, unsigned long long *dmin) {
+  __shared__ uint32_t warp_tot[kBfsThreads / 32];
+  __shared__ uint32_t chunk_tot;
+  __shared__ unsigned long long best;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int32_t root = (int32_t)kept[blockIdx.x].x;
+  const int64_t ncell = kept[blockIdx.x].y;
+  int32_t *ord = order + offs[blockIdx.x];
+  if (tid == 0) {
+    ord[0] = root;
+    a.claim[root] = kClaimDone;
+    best = open_dist_bits(a, root, cx, cy);   // place 0 is sampled
+  }
+  __syncthreads();
+  int64_t lo = 0, hi = 1;   // the current level is ord[lo, hi)
+  while (lo < hi) {
+    // pass 1: every unvisited hole neighbour of the level keeps its smallest claim
+    for (int64_t p0 = lo; p0 < hi; p0 += kBfsThreads / 4) {
+      const int64_t t = p0 + (tid >> 2);
+      if (t < hi) {
+        const int32_t d = open_nb(a, ord[t], tid & 3);
+        if (d >= 0 && a.label[d] == root && __ldcg(a.claim + d) != kClaimDone)
+          atomicMin(a.claim + d, (uint32_t)((t - lo) * 4 + (tid & 3)));
+      }
+    }
+    __syncthreads();
+    // pass 2: the winning claims, ranked in claim order, form the next level
+    int64_t next = hi;
+    for (int64_t p0 = lo; p0 < hi; p0 += kBfsThreads / 4) {
+      const int64_t t = p0 + (tid >> 2);
+      int32_t d = -1;
+      uint32_t flag = 0;
+      if (t < hi) {
+        d = open_nb(a, ord[t], tid & 3);
+        if (d >= 0 && a.label[d] == root && __ldcg(a.claim + d) == (uint32_t)((t - lo) * 4 + (tid & 3))) flag = 1;
+      }
+      // block-wide exclusive scan of flag in thread order (= claim order)
+      uint32_t inc = flag;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+      }
+      if (lane == 31) warp_tot[warp] = inc;
+      __syncthreads();
+      if (warp == 0) {
+        uint32_t w = warp_tot[lane], wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t v = __shfl_up_sync(0xffffffffu, wi, o);
+          if (lane >= o) wi += v;
+        }
+        warp_tot[lane] = wi - w;          // exclusive prefix of the warp totals
+        if (lane == 31) chunk_tot = wi;
+      }
+      __syncthreads();
+      if (flag) {
+        const int64_t pos = next + warp_tot[warp] + inc - 1;
+        if (pos < ncell) {
+          ord[pos] = d;
+          a.claim[d] = kClaimDone;
+          if (pos % 3 == 0) atomicMin(&best, open_dist_bits(a, d, cx, cy));
+        }
+      }
+      next += chunk_tot;
+      __syncthreads();   // warp_tot and chunk_tot are reused by the next chunk
+    }
+    lo = hi;
+    hi = next < ncell ? next : ncell;
+  }
+  if (tid == 0) dmin[blockIdx.x] = best;
+}
+
+// fine cells of the chosen component per coarse cell (:164), then the cells holding at least 5 (:166)
+__global__ void open_sel_kernel(const OpenArgs a, int32_t root, int ny, uint32_t *sel) {
+  const int64_t n = (int64_t)a.nxf * a.nyf;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    if (a.label[c] != root) continue;
+    const int i = (int)(c / a.nyf), j = (int)(c % a.nyf);
+    atomicAdd(sel + (int64_t)(i / 3) * ny + j / 3, 1u);
+  }
+}
+
+__global__ void open_mark_kernel(const uint32_t *sel, int64_t n, uint8_t *opening, OpenOut *out) {
+  uint32_t cnt = 0;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t o = sel[c] >= 5 ? 1 : 0;
+    opening[c] = o;
+    cnt += o;
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&out->n_open, cnt);
+}
+
+cudaError_t open_init(const OpenArgs &a, cudaStream_t st) {
+  open_init_kernel<<<grid_of((int64_t)a.nxf * a.nyf), 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t open_outside_round(const OpenArgs &a, int *changed, cudaStream_t st) {
+  open_outside_kernel<true><<<grid_of(a.nxf), 256, 0, st>>>(a, changed);
+  open_outside_kernel<false><<<grid_of(a.nyf), 256, 0, st>>>(a, changed);
+  return cudaGetLastError();
+}
+
+cudaError_t open_holes(const OpenArgs &a, cudaStream_t st) {
+  open_holes_kernel<<<grid_of((int64_t)a.nxf * a.nyf), 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t open_label_round(const OpenArgs &a, int *changed, cudaStream_t st) {
+  open_label_kernel<true><<<grid_of(a.nxf), 256, 0, st>>>(a, changed);
+  open_label_kernel<false><<<grid_of(a.nyf), 256, 0, st>>>(a, changed);
+  return cudaGetLastError();
+}
+
+cudaError_t open_components(const OpenArgs &a, OpenOut *out, uint2 *kept, uint32_t cap, cudaStream_t st) {
+  const int64_t n = (int64_t)a.nxf * a.nyf;
+  open_size_kernel<<<grid_of(n), 256, 0, st>>>(a);
+  open_roots_kernel<<<grid_of(n), 256, 0, st>>>(a, out, kept, cap);
+  return cudaGetLastError();
+}
+
+cudaError_t open_bfs_click(const OpenArgs &a, const uint2 *kept, const int64_t *offs, int n, int32_t *order,
+                           double cx, double cy, unsigned long long *dmin, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  open_bfs_kernel<<<n, kBfsThreads, 0, st>>>(a, kept, offs, order, cx, cy, dmin);
+  return cudaGetLastError();
+}
+
+cudaError_t open_select(const OpenArgs &a, uint32_t root, int nx, int ny, uint32_t *sel, uint8_t *opening,
+                        OpenOut *out, cudaStream_t st) {
+  open_sel_kernel<<<grid_of((int64_t)a.nxf * a.nyf), 256, 0, st>>>(a, (int32_t)root, ny, sel);
+  open_mark_kernel<<<grid_of((int64_t)nx * ny), 256, 0, st>>>(sel, (int64_t)nx * ny, opening, out);
+  return cudaGetLastError();
 }
 
 }  // namespace abx

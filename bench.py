@@ -12,7 +12,7 @@ GPU.  MLUPS counts fluid-cell updates per second, the reference's definition
 * ``value``  - MLUPS from CUDA-event device time of the K solves (state and
   geometry resident in HBM).
 * ``e2e``    - MLUPS through the C ABI with host buffers: every step prepares
-  the geometry from host triangles (H2D, GPU voxelizer, host flood fill),
+  the geometry from host triangles (H2D, GPU voxelizer, opening search and flood fill),
   runs the solve and reads KPIs, filter map and history back to the host.
 * ``roofline`` - the fused stream+collide kernel (launches without
   averaging): 2*19*4 bytes per fluid cell per launch (float32 storage) over

@@ -41,15 +41,36 @@ def geom_cases():
     cases["outlet_plenum"] = (spec, {"outlet": {"enabled": True, "center": [120.0, 0.0, 90.0], "diameter": 60.0,
                                                 "height": 20.0}})
     cases["click"] = (spec, {"click": [120.0, 77.0, -30.0]})
+    # three holes in the front slice: the stub's and two tubes'; the click picks a tube, or the largest wins
+    cases["tubes_largest"] = (spec, {"_tubes": True})
+    cases["tubes_click_small"] = (spec, {"_tubes": True, "click": [210.0, 70.0, -30.0]})
+    cases["tubes_click_left"] = (spec, {"_tubes": True, "click": [25.0, 64.0, -30.0]})
     return cases
 
 
 CASES = geom_cases()
 
 
+def airbox_with_tubes(spec):
+    """The airbox plus two square tubes, capped at the back, standing in front of its inlet wall beside the
+    stub (disjoint closed solids): the fine slice behind the front-most point then holds three holes, and a
+    click on a tube makes prepare choose that tube's (smaller) hole as the opening."""
+    z0 = -spec.stub
+    z1 = z0 + 10.0
+    parts = [ag.build_airbox(spec)]
+    for x0, y0, w, wall in ((10.0, 50.0, 40.0, 8.0), (195.0, 55.0, 30.0, 8.0)):
+        x1, y1 = x0 + w, y0 + w
+        walls = [(x0, x0 + wall, y0, y1), (x1 - wall, x1, y0, y1), (x0 + wall, x1 - wall, y0, y0 + wall),
+                 (x0 + wall, x1 - wall, y1 - wall, y1)]
+        parts += [ag._box(a, b, c, d, z0, z1 - 3.0).reshape(-1, 9) for a, b, c, d in walls]
+        parts.append(ag._box(x0, x1, y0, y1, z1 - 3.0, z1).reshape(-1, 9))
+    return np.concatenate(parts).astype(np.float32)
+
+
 def prep_both(spec, extra=None, **kw):
-    tris = ag.build_airbox(spec)
-    p = {**spec.prepare_params(), **(extra or {})}
+    extra = dict(extra or {})
+    tris = airbox_with_tubes(spec) if extra.pop("_tubes", False) else ag.build_airbox(spec)
+    p = {**spec.prepare_params(), **extra}
     og = O.prepare(tris, p, keep_fine=kw.get("keep_fine", False), max_cells=kw.get("max_cells", 4.5e6))
     g = E.prepare({"tris": tris, **p, "maxCells": kw.get("max_cells", 4.5e6)})
     return og, g
@@ -192,13 +213,17 @@ def test_f32_full_run_within_tolerance():
         assert res["metrics"][k] == pytest.approx(m_o[k], rel=5e-3), k
 
 
-@pytest.mark.parametrize("name", ["no_opening", "same_axis", "grid_too_large", "bad_outlet", "lid_too_low"])
+@pytest.mark.parametrize("name", ["no_opening", "same_axis", "grid_too_large", "bad_outlet", "lid_too_low",
+                                  "opening_too_small"])
 def test_prepare_errors_match_reference(name):
     spec = ag.config1_spec()
     tris = ag.build_airbox(spec)
     p = spec.prepare_params()
     kw = {}
-    if name == "no_opening":
+    if name == "opening_too_small":                  # a click on the small tube's hole at 5 mm cells
+        tris = airbox_with_tubes(spec)
+        p.update(click=[210.0, 70.0, -30.0], dx=5.0)
+    elif name == "no_opening":
         p["inletAxis"], p["inletSign"] = 0, -1        # a side face without a hole
     elif name == "same_axis":
         p["inletAxis"] = 1
