@@ -97,8 +97,12 @@ def makeFrame(p: dict) -> Frame:
 class Geometry:
     """The prepare() result (src/engine.js:226-233), device-resident.
 
-    Scalars are read at once; the masks (solid, fluid, opening, outlet) and
-    xc/dc/zc are copied to the host on first access."""
+    Scalars are read at once; each of the masks (solid, fluid, opening, outlet)
+    and xc/dc/zc is copied to the host on its first access, on its own (the
+    N-byte masks only when asked for)."""
+
+    # abx_geom_get_masks argument order
+    _ARRAYS = ("solid", "fluid", "opening", "outlet", "xc", "dc", "zc")
 
     def __init__(self, handle: C.c_void_p, p: dict):
         self._h = handle
@@ -110,26 +114,26 @@ class Geometry:
         self.top, self.jm, self.nf, self.pleat = info.top, info.jm, info.nf, info.pleat
         self.mn, self.mx = list(info.mn), list(info.mx)
         self.origin = list(info.origin)
-        self._masks = None
+        self._arrays = {}
 
-    def _load_masks(self):
-        if self._masks is None:
-            N, nx, ny, nz = self.N, self.nx, self.ny, self.nz
-            m = {k: np.empty(N, np.uint8) for k in ("solid", "fluid", "outlet")}
-            m["opening"] = np.empty(nx * ny, np.uint8)
-            m["xc"], m["dc"], m["zc"] = np.empty(nx, np.float32), np.empty(ny, np.float32), np.empty(nz, np.float32)
-            _check(A.load().abx_geom_get_masks(self._h, _ptr(m["solid"]), _ptr(m["fluid"]), _ptr(m["opening"]),
-                                               _ptr(m["outlet"]), _ptr(m["xc"]), _ptr(m["dc"]), _ptr(m["zc"])))
-            self._masks = m
-        return self._masks
+    def _array(self, key: str) -> np.ndarray:
+        a = self._arrays.get(key)
+        if a is None:
+            n, dt = {"solid": (self.N, np.uint8), "fluid": (self.N, np.uint8), "outlet": (self.N, np.uint8),
+                     "opening": (self.nx * self.ny, np.uint8), "xc": (self.nx, np.float32),
+                     "dc": (self.ny, np.float32), "zc": (self.nz, np.float32)}[key]
+            a = np.empty(n, dt)
+            _check(A.load().abx_geom_get_masks(self._h, *[_ptr(a) if k == key else None for k in self._ARRAYS]))
+            self._arrays[key] = a
+        return a
 
-    solid = property(lambda self: self._load_masks()["solid"])
-    fluid = property(lambda self: self._load_masks()["fluid"])
-    opening = property(lambda self: self._load_masks()["opening"])
-    outlet = property(lambda self: self._load_masks()["outlet"])
-    xc = property(lambda self: self._load_masks()["xc"])
-    dc = property(lambda self: self._load_masks()["dc"])
-    zc = property(lambda self: self._load_masks()["zc"])
+    solid = property(lambda self: self._array("solid"))
+    fluid = property(lambda self: self._array("fluid"))
+    opening = property(lambda self: self._array("opening"))
+    outlet = property(lambda self: self._array("outlet"))
+    xc = property(lambda self: self._array("xc"))
+    dc = property(lambda self: self._array("dc"))
+    zc = property(lambda self: self._array("zc"))
 
     def fine(self) -> np.ndarray:
         """voxelize()'s fine grid (3x per axis), recomputed on the GPU."""
