@@ -844,10 +844,16 @@ static int run_steps(abx_sim *s, int n, bool acc) {
   if (n <= 0) return ABX_OK;
   if (!s->use_graphs) {
     const StepArgs a = step_args(*s);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (s->timing) {
+      e0 = next_event(s); e1 = next_event(s);
+      if (e0 && e1) { cudaEventRecord(e0, s->st); s->ev_kind.push_back(acc ? 1 : 0); s->ev_nsteps.push_back(n); }
+    }
     for (int i = 0; i < n; i++) {
       CK(launch_step(s->p.storage, s->form == 0, acc, s->has_ns, a, s->tma.ready ? &s->tma : nullptr, s->st), "run: step");
       s->form ^= 1;
     }
+    if (e0 && e1) cudaEventRecord(e1, s->st);
     s->step += n;
     if (acc) s->nacc += n;
     s->step_launches += n;
