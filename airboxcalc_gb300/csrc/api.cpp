@@ -280,6 +280,7 @@ static int find_opening(abx_geom &g, const abx_prepare_params *p, const uint8_t 
     std::vector<int> idx(n);
     for (int b = 0; b < n; b++) idx[b] = b;
     std::sort(idx.begin(), idx.end(), [&](int x, int y) { return kv[x].x < kv[y].x; });
+    root = kv[idx[0]].x;   // comps[0] stays chosen when no distance is below Infinity (a non-finite click)
     double bd = INFINITY;
     for (int b : idx) {
       double d;

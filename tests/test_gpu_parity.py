@@ -45,6 +45,8 @@ def geom_cases():
     cases["tubes_largest"] = (spec, {"_tubes": True})
     cases["tubes_click_small"] = (spec, {"_tubes": True, "click": [210.0, 70.0, -30.0]})
     cases["tubes_click_left"] = (spec, {"_tubes": True, "click": [25.0, 64.0, -30.0]})
+    # no distance compares below Infinity: the first component in scan order stays chosen, not the largest
+    cases["tubes_click_nan"] = (spec, {"_tubes": True, "click": [float("nan"), 70.0, -30.0]})
     return cases
 
 
