@@ -9,6 +9,7 @@
 #include <cudaTypedefs.h>
 
 #include <cstring>
+#include <utility>
 
 #ifndef ABX_TMA_STAGES
 #define ABX_TMA_STAGES 3
@@ -16,11 +17,31 @@
 
 namespace abx {
 
+// Step kernels are launched with programmatic stream serialization (ABX_PDL=0: plain launches): the next
+// step may be launched while the previous one finishes; the kernels wait for it before touching memory.
+#ifndef ABX_PDL
+#define ABX_PDL 1
+#endif
+template <class... KArgs, class... Args>
+static cudaError_t launch_step_kernel(void (*kern)(KArgs...), unsigned grid, cudaStream_t st, Args &&...args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = ABX_PDL ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
 template <int K>
 static cudaError_t step_k(bool odd, bool acc, bool has_ns, const StepArgs &a, cudaStream_t st) {
   if (a.nseg == 0) return cudaSuccess;
-  const dim3 grid(step_grid(a.nseg)), block(256);
-#define ABX_L(O, A, N) aa_step_kernel<K, O, A, N><<<grid, block, 0, st>>>(a)
+  const unsigned grid = step_grid(a.nseg);
+#define ABX_L(O, A, N) return launch_step_kernel(aa_step_kernel<K, O, A, N>, grid, st, a)
   if (odd) {
     if (acc) { if (has_ns) ABX_L(true, true, true); else ABX_L(true, true, false); }
     else { if (has_ns) ABX_L(true, false, true); else ABX_L(true, false, false); }
@@ -38,13 +59,11 @@ static cudaError_t step_batch_k(bool odd, bool acc, const BatchParams &P, const 
                                 uint32_t grid, cudaStream_t st) {
   if (t1 <= t0) return cudaSuccess;
   if (odd) {
-    if (acc) aa_step_batch_kernel<K, true, true, SPW, MINB><<<grid, 256, 0, st>>>(P, tiles, t0, t1);
-    else aa_step_batch_kernel<K, true, false, SPW, MINB><<<grid, 256, 0, st>>>(P, tiles, t0, t1);
-  } else {
-    if (acc) aa_step_batch_kernel<K, false, true, SPW, MINB><<<grid, 256, 0, st>>>(P, tiles, t0, t1);
-    else aa_step_batch_kernel<K, false, false, SPW, MINB><<<grid, 256, 0, st>>>(P, tiles, t0, t1);
+    if (acc) return launch_step_kernel(aa_step_batch_kernel<K, true, true, SPW, MINB>, grid, st, P, tiles, t0, t1);
+    return launch_step_kernel(aa_step_batch_kernel<K, true, false, SPW, MINB>, grid, st, P, tiles, t0, t1);
   }
-  return cudaGetLastError();
+  if (acc) return launch_step_kernel(aa_step_batch_kernel<K, false, true, SPW, MINB>, grid, st, P, tiles, t0, t1);
+  return launch_step_kernel(aa_step_batch_kernel<K, false, false, SPW, MINB>, grid, st, P, tiles, t0, t1);
 }
 
 template <int K>

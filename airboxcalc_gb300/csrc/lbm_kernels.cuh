@@ -154,8 +154,18 @@ __device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, cons
 #define ABX_STEP_PERSIST 1
 #endif
 
+// Programmatic dependent launch between consecutive steps: a step kernel waits until the previous kernel of its
+// stream has completed and its writes are visible before it touches memory, then lets the next kernel be
+// launched as soon as all of its own blocks are running, so one step's launch overlaps the previous step's tail.
+// Both are no-ops for a kernel launched without the programmatic-serialization attribute.
+__device__ __forceinline__ void step_dependency_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 template <int K, bool ODD, bool ACC, bool HAS_NS>
 __global__ void __launch_bounds__(256, ABX_STEP_MINBLOCKS) aa_step_kernel(const StepArgs a) {
+  step_dependency_wait();
 #if ABX_STEP_PERSIST
   const uint32_t nw = gridDim.x * 8u;
   for (uint32_t s = blockIdx.x * 8u + (threadIdx.x >> 5); s < a.nseg; s += nw)
@@ -194,6 +204,7 @@ template <int K, bool ODD, bool ACC, int SPW, int MINB>
 __global__ void __launch_bounds__(256, MINB)
     aa_step_batch_kernel(const __grid_constant__ BatchParams P, const uint2 *__restrict__ tiles, uint32_t t0,
                          uint32_t t1) {
+  step_dependency_wait();
   const uint32_t n = t1 - t0;
   for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
     const uint2 tile = tiles[t0 + ((ABX_STEP_ALTERNATE && ODD) ? n - 1u - i : i)];
