@@ -15,8 +15,8 @@ pin for the compute core:
   the 6-connected flood from the inlet, saved as the solid and fluid masks;
 * ``report`` (airbox_cfd.py:296-314) - gamma, gamma core, the core shares under
   50 % / over 150 %, reverse flow, peak-to-mean and zeta, computed by the CLI on
-  its own averaged fields of a 60-step run (fields and KPIs both stored), which
-  pins the formulas of evaluate() (src/engine.js:632-660).
+  its own averaged fields of a 60-step run (fields and KPIs both stored, for
+  two geometries), which pins the formulas of evaluate() (src/engine.js:632-660).
 
 The JS path stores voxel hits as float32 and tests ``ceil(z/h - 0.5)``, the
 Python path keeps float64 and tests ``zc >= z``; the two agree unless a face
@@ -56,6 +56,9 @@ CASES = {
                                  dx=2.5, baffle={"z": 33.71, "x0": 40.13, "x1": 93.24, "y0": 55.07})),
 }
 
+
+# geometries whose report() KPIs are stored (on the CLI's own averaged fields of a 60-step run)
+REPORT_CASES = ("small_baffle", "wide_low")
 
 # report() result keys (airbox_cfd.py:360-363) in the order stored in the fixture
 REPORT_KPIS = ("gamma", "gamma_ohne_randzellen", "anteil_unter_50pct_kern", "anteil_ueber_150pct_kern",
@@ -142,7 +145,7 @@ def main():
             shape = tuple(int(math.ceil((mx[i] - origin[i] + h) / h)) for i in range(3))
             fine = R.voxelize(T, origin, tuple(s * 3 for s in shape), h / 3)
             masks = run_main(R, stl, spec, td)
-            if name == "small_baffle":
+            if name in REPORT_CASES:
                 # report()'s KPIs (airbox_cfd.py:301-314) on the CLI's own averaged fields of a 60-step run
                 run = run_main(R, stl, spec, td, steps=60, avg=20)
                 for k in ("ux", "uy", "uz", "rho"):

@@ -84,11 +84,11 @@ def test_voxelizer_and_masks_match_reference(name):
     assert np.array_equal(g.fluid(), np.unpackbits(GOLD[f"vox_{name}_fluid"])[:n])
 
 
-def test_evaluate_formulas_match_reference_report():
+@pytest.mark.parametrize("name", ["small_baffle", "wide_low"])
+def test_evaluate_formulas_match_reference_report(name):
     """report() of the reference's Python CLI (airbox_cfd.py:296-314) on its own averaged fields of a 60-step run
     against the oracle's evaluate() (src/engine.js:632-660) on the same fields: the KPI formulas agree.  The CLI
     sums float32 arrays with numpy's pairwise float32 sums where engine.js sums in float64, hence the tolerance."""
-    name = "small_baffle"
     spec = ag.AirboxSpec(**SPECS[name])
     g = O.prepare(ag.build_airbox(spec), spec.prepare_params())
     S = O.OracleSim(g, dict(K=3.0, aniso=10.0, u=0.06, tau=0.51))
