@@ -97,3 +97,26 @@ def test_prepare_rejects_grids_beyond_32_bit_offsets_before_any_gpu_work():
     with pytest.raises(E.AirboxError) as ei:
         E.prepare({**p, "maxCells": 4.5e6})               # the reference's own cap comes first
     assert ei.value.code == A.ERR_GRID_TOO_LARGE and "Gitter zu groß" in str(ei.value)
+
+
+def test_geometry_copies_each_array_on_its_own(monkeypatch):
+    """The Python Geometry asks abx_geom_get_masks for one array per call, on first access only: reading the
+    coordinates (as evaluate() does) never copies the N-byte masks."""
+    from airboxcalc_gb300 import engine as E
+    calls = []
+
+    class FakeLib:
+        def abx_geom_get_masks(self, h, *ptrs):
+            asked = [k for k, p in zip(E.Geometry._ARRAYS, ptrs) if p is not None]
+            calls.append(asked)
+            return A.OK
+
+    monkeypatch.setattr(A, "load", lambda *a, **k: FakeLib())
+    g = object.__new__(E.Geometry)
+    g._h, g.N, g.nx, g.ny, g.nz, g._arrays = C.c_void_p(1), 6 * 5 * 4, 6, 5, 4, {}
+    assert g.xc.shape == (6,) and g.zc.shape == (4,) and g.dc.shape == (5,)
+    assert g.xc is g.xc and g.opening.shape == (30,)
+    assert calls == [["xc"], ["zc"], ["dc"], ["opening"]]
+    assert g.fluid.shape == (120,) and g.fluid.dtype == np.uint8
+    assert calls[-1] == ["fluid"] and len(calls) == 5
+    g._h = None                      # a stand-in handle: nothing to free
