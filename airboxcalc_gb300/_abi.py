@@ -21,7 +21,7 @@ ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_OUT_OF_MEMORY = 20, 21, 22
 STORAGE = {"f32": 0, "f32exact": 1, "f16": 2, "bf16": 3, "f64": 4}
 
 # Every symbol include/airbox.h declares.
-ABI_VERSION = 2  # include/airbox.h ABX_ABI_VERSION: the structures below follow that version
+ABI_VERSION = 3  # include/airbox.h ABX_ABI_VERSION: the structures below follow that version
 MAX_LINE_POINTS = 2001  # include/airbox.h ABX_MAX_LINE_POINTS
 
 EXPORTS = [
@@ -61,7 +61,11 @@ class GeomInfo(C.Structure):
 
 class RunParams(C.Structure):
     _fields_ = [("K", C.c_double), ("aniso", C.c_double), ("u", C.c_double), ("tau", C.c_double),
-                ("steps", C.c_int), ("avg", C.c_int), ("every", C.c_int), ("storage", C.c_int)]
+                ("steps", C.c_int), ("avg", C.c_int), ("every", C.c_int), ("storage", C.c_int),
+                ("flags", C.c_uint)]
+
+
+RUN_ALLOW_BF16 = 1  # include/airbox.h ABX_RUN_ALLOW_BF16
 
 
 class SimInfo(C.Structure):

@@ -42,7 +42,8 @@ class Batch:
         for i, p in enumerate(params):
             rp[i] = A.RunParams(K=p["K"], aniso=p["aniso"], u=p["u"], tau=p["tau"], steps=int(p["steps"]),
                                 avg=int(p["avg"]), every=int(p.get("every", 1) or 1),
-                                storage=A.STORAGE[p.get("storage", "f32")])
+                                storage=A.STORAGE[p.get("storage", "f32")],
+                                flags=A.RUN_ALLOW_BF16 if p.get("allowBf16") else 0)
         h = C.c_void_p()
         E._check(A.load().abx_batch_create(hs, rp, n, C.byref(h)))
         self._h = h

@@ -22,6 +22,8 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <cuda.h>
+
 #include <mutex>
 
 #include "lbm_iface.h"
@@ -344,7 +346,41 @@ constexpr size_t kStaticScratchBytes = 32u << 20;   // 32 MiB, held by every GPU
 static __device__ __align__(256) unsigned char g_vox_scratch[kStaticScratchBytes];
 
 static std::mutex g_scratch_mu;
-static void *g_scratch_addr[256];   // device address of g_vox_scratch per device ordinal (set once)
+// Device address of g_vox_scratch per device ordinal, and the id of the context it was resolved in.  A
+// cudaDeviceReset (or any other end of the primary context) loads the module again at a new address, so the
+// cached address is used only while the current context is the one it came from; otherwise, and after any
+// failed call, it is resolved again.
+struct ScratchSlot {
+  void *addr = nullptr;
+  unsigned long long ctx = 0;
+};
+static ScratchSlot g_scratch_slot[256];
+
+// Unique id of the calling thread's current context (0 when it cannot be read): cuCtxGetCurrent and
+// cuCtxGetId through the runtime's driver entry points (no link against libcuda).
+static unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrent)p;
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (GetId)p;
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 static size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
@@ -359,20 +395,36 @@ int voxelize_static(const float *d_tris, size_t nfloats, const double origin[3],
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= 256) return err(21, "voxelize_static: no current CUDA device (%lld, %lld)", e, dev);
+  // cudaSetDevice makes the device's primary context current (initialising it if needed), so that its id
+  // can be read; no allocation is involved
+  e = cudaSetDevice(dev);
+  if (e != cudaSuccess) return err(21, "voxelize_static: cudaSetDevice failed (error %lld, device %lld)", e, dev);
+  const unsigned long long ctx = current_context_id();
   void *base = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
-      // the symbol's name is only a host-side stand-in: resolve its device address
-      // once per device, with that device current
-      e = cudaGetSymbolAddress(&g_scratch_addr[dev], g_vox_scratch);
+    ScratchSlot &slot = g_scratch_slot[dev];
+    if (!slot.addr || ctx == 0 || slot.ctx != ctx) {
+      // the symbol's name is only a host-side stand-in: resolve its device address with the device current,
+      // once per device and context
+      slot.addr = nullptr;
+      e = cudaGetSymbolAddress(&slot.addr, g_vox_scratch);
       if (e != cudaSuccess) {
-        g_scratch_addr[dev] = nullptr;
+        slot.addr = nullptr;
         return err(21, "voxelize_static: cudaGetSymbolAddress failed (error %lld, device %lld)", e, dev);
       }
+      slot.ctx = ctx;
     }
-    base = g_scratch_addr[dev];
+    base = slot.addr;
   }
+  // any failure below drops the cached address, so that the next call resolves it again
+  auto drop = [&](int rc) {
+    if (rc) {
+      std::lock_guard<std::mutex> lock(g_scratch_mu);
+      g_scratch_slot[dev].addr = nullptr;
+    }
+    return rc;
+  };
   const int64_t ncol = (int64_t)nx * ny, ntri = (int64_t)(nfloats / 9);
   const int64_t tmp_n = (ncol > ntri ? ncol : ntri) / kScanTile + 2;
   // fixed part of the scratch: triangle records, prefix sums, column counters and offsets
@@ -397,7 +449,7 @@ int voxelize_static(const float *d_tris, size_t nfloats, const double origin[3],
   uint8_t *slice = (uint8_t *)(S + o_sli);
   float *hits = (float *)(S + o_hit);
   int64_t W = 0, H = 0;
-#define ABX_SC(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return err(21, "voxelize_static: CUDA error %lld at step %lld", e_, __LINE__); } while (0)
+#define ABX_SC(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return drop(err(21, "voxelize_static: CUDA error %lld at step %lld", e_, __LINE__)); } while (0)
   // the scratch keeps the previous call's contents: zero what the passes accumulate into
   ABX_SC(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (size_t)ncol, st));
   ABX_SC(cudaMemsetAsync(cursor, 0, sizeof(uint32_t) * (size_t)ncol, st));

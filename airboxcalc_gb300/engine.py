@@ -202,7 +202,8 @@ class Simulation:
         self.p = dict(p)
         rp = A.RunParams(K=p["K"], aniso=p["aniso"], u=p["u"], tau=p["tau"], steps=int(p.get("steps", 0)),
                          avg=int(p.get("avg", 0)), every=int(p.get("every", 1) or 1),
-                         storage=A.STORAGE[p.get("storage", "f32")])
+                         storage=A.STORAGE[p.get("storage", "f32")],
+                         flags=A.RUN_ALLOW_BF16 if p.get("allowBf16") else 0)
         self._ns = None if ns is None else np.ascontiguousarray(ns, np.float32)
         h = C.c_void_p()
         _check(A.load().abx_sim_create(g._h, C.byref(rp), _ptr(self._ns), C.byref(h)))

@@ -1,19 +1,24 @@
 """Benchmark of the airbox compute core on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload config2|config1|config3] [--storage f32|f16|bf16]
+                    [--workload config3|config2|config1] [--storage f32|f16] [--block B]
 
-One bench step is one whole solve of the workload's airbox: the full
-simulate() step loop (6000 LBM steps, the last 2000 averaged, a progress
-probe every 150 steps) and evaluate(), on a geometry already prepared on the
-GPU.  MLUPS counts fluid-cell updates per second, the reference's definition
-(src/engine.js:338).
+Default workload: config3, the largest single-GPU configuration (a
+512x256x384-cell seeded airbox at dx 0.6 mm, 39.2 M fluid cells, tau 0.505,
+u 0.05, 20000 LBM steps with the last 5000 averaged).
 
-* ``value``  - MLUPS from CUDA-event device time of the K solves (state and
-  geometry resident in HBM).
-* ``e2e``    - MLUPS through the C ABI with host buffers: every step prepares
-  the geometry from host triangles (H2D, GPU voxelizer, opening search and flood fill),
-  runs the solve and reads KPIs, filter map and history back to the host.
+One bench step is one block of that solve's schedule: B LBM steps (default
+16) of which the last round(B * avg / steps) add to the time averages (4 of
+16: the 5000/20000 share), on the same continuing state.  MLUPS counts
+fluid-cell updates per second, the reference's definition (src/engine.js:338).
+
+* ``value``  - MLUPS from CUDA-event device time of the K blocks (state and
+  geometry resident in HBM; the state is 4.6 GB, 36x the L2, so no flush is
+  needed between blocks).
+* ``e2e``    - MLUPS of whole solves through the C ABI with host buffers: each
+  prepares the geometry from host triangles (H2D, GPU voxelizer, opening
+  search and flood fill), runs the full schedule (all 20000 steps, progress
+  probes every 500) and reads KPIs, filter map and history back.
 * ``roofline`` - the fused stream+collide kernel (launches without
   averaging): 2*19*4 bytes per fluid cell per launch (float32 storage) over
   its CUDA-event launch time, against the measured HBM copy bandwidth.
@@ -22,8 +27,9 @@ GPU.  MLUPS counts fluid-cell updates per second, the reference's definition
 
 ``--impl reference`` times the reference's CPU algorithm (no JavaScript
 runtime exists on this machine, so the C restatement stands in for
-src/engine.js's cpuStep) with every host core, on the same workload.
-Under torchrun the solves run as independent replicas, one per GPU.
+src/engine.js's cpuStep) with every host core, on the same workload and the
+same blocks (same ``config``).  Under torchrun the runs are independent
+replicas, one per GPU.
 """
 from __future__ import annotations
 
@@ -35,6 +41,8 @@ import subprocess
 import sys
 import threading
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -53,13 +61,14 @@ def workload(name: str):
         return spec, dict(RUN), "config2: seeded airbox (seed 1000), dx 1.5 mm, 6000 steps / 2000 averaged"
     if name == "config3":
         spec = ag.grid_spec(512, 256, 384, dx=0.6)
-        run = dict(RUN, tau=0.505, u=0.05, steps=20000, avg=5000, every=500)
+        run = dict(RUN, tau=0.505, u=0.05, steps=20000, avg=5000, every=500)  # every: src/ui.html:502 rule
         return spec, run, "config3: 512x256x384-cell airbox, dx 0.6 mm, 20000 steps / 5000 averaged"
     raise SystemExit(f"unknown workload {name}")
 
 
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
+    """nvidia-smi clock/throttle samples every 50 ms; only samples inside the marked timed windows count."""
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
@@ -67,29 +76,41 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.rows = []
+        self.windows = []
         self.proc = None
         self.thread = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (FileNotFoundError, OSError):
             self.proc = None
             return
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        t0 = time.perf_counter()
+        while not self.rows and time.perf_counter() - t0 < 5.0:   # first sample in before timing starts
+            time.sleep(0.02)
 
     def _read(self):
         for line in self.proc.stdout:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) >= 7:
-                self.rows.append(parts)
+                self.rows.append((time.perf_counter(), parts))
+
+    def begin(self):
+        self.windows.append([time.perf_counter(), None])
+
+    def end(self):
+        if self.windows and self.windows[-1][1] is None:
+            self.windows[-1][1] = time.perf_counter()
 
     def stop(self):
         if self.proc is None:
             return None
+        time.sleep(0.1)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -97,10 +118,11 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        rows = [r for t, r in self.rows if any(a <= t <= (b or a) + 0.06 for a, b in self.windows)]
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i].lower() == "active"})
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
@@ -199,7 +221,7 @@ KPI = ("gamma", "gammaCore", "lowCore", "maxToMean", "zeta")
 def solve(g, run, storage, timing=True):
     """One whole simulate() + evaluate() on the GPU; returns (metrics, averages, device ms)."""
     from airboxcalc_gb300 import engine as E
-    S = E.Simulation(g, {**run, "storage": storage})
+    S = E.Simulation(g, {**run, "storage": storage, "allowBf16": True})
     S.set_timing(timing)
     S.run()
     res = S.evaluate()
@@ -230,6 +252,37 @@ def study_precision(spec, run, desc, storages=("f64", "f32exact", "f32", "f16", 
                      "kpi": {k: round(m[k], 6) for k in KPI}, "rel_err_vs_f64": {k: float(f"{v:.3e}") for k, v in err.items()},
                      "rel_l2_u_vs_f64": float(f"{l2u:.3e}"), "rel_l2_rho_minus_1_vs_f64": float(f"{l2r:.3e}")})
         print(json.dumps(rows[-1]), flush=True)
+    return rows
+
+
+def study_decorrelation(spec, run, desc, storages=("f32", "f16"), checkpoints=(500, 1000, 2000, 4000, 8000),
+                        window=100):
+    """How the float32 / float16 fields drift from the float64 run's over a solve: all runs start from w_i on
+    the same airbox; at each checkpoint every run averages the next `window` steps, and the relative L2
+    difference of those averages (u, and rho - 1) to the float64 run's is reported.  A precision bias shows as
+    a difference present from the first checkpoints on; the divergence of unsteady trajectories as one that
+    starts at round-off level and grows with the step count."""
+    import numpy as np
+    from airboxcalc_gb300 import airboxgen as ag
+    from airboxcalc_gb300 import engine as E
+    g = E.prepare({"tris": ag.build_airbox(spec), **spec.prepare_params(), "maxCells": 1e10})
+    sims = {st: E.Simulation(g, {**run, "storage": st}) for st in ("f64",) + tuple(storages)}
+    done = 0
+    rows = []
+    for c in checkpoints:
+        for S in sims.values():
+            S.step(c - done)
+            S.clear_acc()
+            S.step(window, True)
+        done = c + window
+        ref = sims["f64"].get_acc().reshape(4, -1).astype(np.float64)
+        row = {"study": "decorrelation", "workload": desc, "step": c, "window": window}
+        for st in storages:
+            a = sims[st].get_acc().reshape(4, -1).astype(np.float64)
+            row[st] = {"rel_l2_u": float(f"{np.linalg.norm(a[:3] - ref[:3]) / np.linalg.norm(ref[:3]):.3e}"),
+                       "rel_l2_rho_minus_1": float(f"{np.linalg.norm(a[3] - ref[3]) / np.linalg.norm(ref[3] - 1):.3e}")}
+        rows.append(row)
+        print(json.dumps(row), flush=True)
     return rows
 
 
@@ -435,13 +488,13 @@ def study_batch(n: int = 64, storage: str = "f16", quiet: bool = False):
             continue
         t = S.timing()
         t32 += t["run_ms"]
-        S16 = E.Simulation(g, dict(run, storage=storage))
+        S16 = E.Simulation(g, dict(run, storage=storage, allowBf16=True))
         S16.set_timing(True)
         S16.run()
         t16 += S16.timing()["run_ms"]
         del S, S16
         geoms.append(g)
-        params.append(dict(run, storage=storage))
+        params.append(dict(run, storage=storage, allowBf16=True))
         rows.append({"seed": seed, "dx": dx, "K": K, "NF": g.nf, "ref": ref})
         cells += g.nf
     B = BT.Batch(geoms, params)
@@ -477,19 +530,85 @@ def study_batch(n: int = 64, storage: str = "f16", quiet: bool = False):
     return out
 
 
+def block_shape(run, block: int):
+    """(plain, averaged) LBM steps of one bench step: the schedule's averaged share of `block` steps."""
+    nacc = max(1, round(block * run["avg"] / run["steps"])) if run["avg"] > 0 else 0
+    return block - nacc, nacc
+
+
+def bench_config(desc, grid, NF, run, block, storage, ws):
+    """The `config` object of the bench line; both arms print the same one."""
+    plain, nacc = block_shape(run, block)
+    state_bytes = (19 + 4) * 4 * NF   # float32 populations (one A-A array) and averages of the fluid cells
+    return {"workload": desc, "grid": list(grid), "NF": int(NF), "schedule": {"steps": run["steps"],
+            "avg": run["avg"], "every": run["every"], "tau": run["tau"], "u": run["u"]},
+            "lbm_steps_per_bench_step": block, "averaged_steps_per_bench_step": nacc, "storage": storage,
+            "state_bytes": int(state_bytes),
+            "l2": "state larger than the 129 MB L2, no flush needed" if state_bytes > 129e6 else "state smaller than L2",
+            "e2e": "whole solves (prepare from host triangles, full schedule, evaluate and read-back)",
+            "parallelism": f"replicas x{ws}"}
+
+
+def reference_arm(a, spec, run, desc, rank):
+    """--impl reference: the C restatement of cpuStep (src/engine.js:266-321) on every host core, on the same
+    airbox and the same blocks of the schedule as our arm."""
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    from airboxcalc_gb300 import airboxgen as ag
+    O.build()
+    cores = os.cpu_count() or 1
+    og = O.prepare(ag.build_airbox(spec), spec.prepare_params(), max_cells=1e10)
+    S = O.OracleSim(og, run)
+    plain, nacc = block_shape(run, a.block)
+    f = S.f0()
+    acc = np.zeros(4 * S.NF, np.float32)
+
+    def block():
+        nonlocal f
+        for _ in range(plain):
+            f = S.step(f, kind="f32", nthreads=cores)
+        for _ in range(nacc):
+            f = S.step(f, acc=acc, kind="f32", nthreads=cores)
+
+    for _ in range(a.warmup):
+        block()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        block()
+    el = time.perf_counter() - t0
+    v = S.NF * a.block * a.steps / el / 1e6
+    sample = (f"{a.block} LBM steps per bench step ({plain} plain, {nacc} adding to the averages) of the workload "
+              f"airbox (NF={S.NF}) on a continuing state from w_i")
+    line = {"metric": METRIC, "value": round(v, 3), "unit": "MLUPS", "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": round(el / a.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64-locals/f32-storage", "data": "synthetic",
+            "config": bench_config(desc, (og.nx, og.ny, og.nz), S.NF, run, a.block, "f32", a.gpus),
+            "impl": "reference",
+            "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": cores, "kind": "port",
+                             "sample": sample + "; C restatement of src/engine.js cpuStep (no JavaScript "
+                             "runtime here or on the GPU host), OpenMP over cells"},
+            "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3"])
-    ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
+    ap.add_argument("--workload", default="config3", choices=["config1", "config2", "config3"])
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16"])
+    ap.add_argument("--block", type=int, default=16, help="LBM steps per bench step")
+    ap.add_argument("--e2e-solves", type=int, default=2, help="whole end-to-end solves timed for e2e")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-warm-start", action="store_true", help="skip the warm-start sample of the bench line")
-    ap.add_argument("--study", choices=["precision", "converge", "warmstart", "batch"], default=None,
+    ap.add_argument("--study", choices=["precision", "converge", "warmstart", "batch", "decorrelation"], default=None,
                     help="instead of the bench line: KPI error per storage vs float64, steps/time to converged "
-                         "KPIs, or the learned warm start on held-out airboxes")
+                         "KPIs, the learned warm start on held-out airboxes, the batched variant table, or the "
+                         "growth of the float32/float16 vs float64 field difference over a solve")
     ap.add_argument("--seeds", default="6000:6200", help="held-out seed range a:b of --study warmstart")
     ap.add_argument("--storages", default="f64,f32exact,f32,f16,bf16", help="storages of --study precision")
     ap.add_argument("--weights", default=None, help="warm-start network weights (.npz)")
@@ -502,50 +621,23 @@ def main():
     if a.study == "converge":
         study_converge(spec, run, desc)
         return 0
+    if a.study == "decorrelation":
+        study_decorrelation(spec, run, desc)
+        return 0
     if a.study == "batch":
-        study_batch(64, a.storage if a.storage != "f32" else "f16")
+        study_batch(64, "f16")
         return 0
     if a.study == "warmstart":
         from airboxcalc_gb300 import warmstart as W
         lo, hi = map(int, a.seeds.split(":"))
         study_warmstart(range(lo, hi), a.weights or W.WEIGHTS)
         return 0
-
     if a.impl == "reference":
-        if rank != 0:
-            return 0
-        from oracle import oracle as O
-        from airboxcalc_gb300 import airboxgen as ag
-        O.build()
-        cores = os.cpu_count() or 1
-        og = O.prepare(ag.build_airbox(spec), spec.prepare_params(), max_cells=1e10)
-        S = O.OracleSim(og, run)
-        f = S.f0()
-        per_step = 10
-        for _ in range(a.warmup):
-            for _ in range(per_step):
-                f = S.step(f, kind="f32", nthreads=cores)
-        t0 = time.perf_counter()
-        for _ in range(a.steps):
-            for _ in range(per_step):
-                f = S.step(f, kind="f32", nthreads=cores)
-        el = time.perf_counter() - t0
-        v = S.NF * per_step * a.steps / el / 1e6
-        sample = f"{per_step} LBM steps of the workload airbox per bench step (NF={S.NF}), from w_i"
-        line = {"metric": METRIC, "value": round(v, 3), "unit": "MLUPS", "n_gpus": a.gpus, "steps": a.steps,
-                "warmup": a.warmup, "ms_per_step": round(el / a.steps * 1e3, 3), "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64-locals/f32-storage", "data": "synthetic",
-                "config": {"workload": desc, "lbm_steps_per_bench_step": per_step, "NF": S.NF},
-                "impl": "reference",
-                "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": cores, "kind": "port",
-                                 "sample": sample + "; C restatement of src/engine.js cpuStep (no JavaScript "
-                                 "runtime here), OpenMP over cells"},
-                "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
-        return 0
+        return reference_arm(a, spec, run, desc, rank)
+    return ours_arm(a, spec, run, desc, ws, rank, local)
 
-    # ---------------------------------------------------------------- our arm
-    from airboxcalc_gb300 import _abi
+
+def ours_arm(a, spec, run, desc, ws, rank, local):
     from airboxcalc_gb300 import airboxgen as ag
     from airboxcalc_gb300 import engine as E
     dist = Dist(ws)
@@ -557,70 +649,58 @@ def main():
     S = E.Simulation(g, runp)
     NF = S.NF
     S.set_timing(True)
+    plain, nacc = block_shape(run, a.block)
 
-    def solve():
-        S.reset()
-        S.run()
-        return S.evaluate()
+    def block():
+        S.step(plain)
+        if nacc:
+            S.step(nacc, accumulate=True)
 
     for _ in range(a.warmup):
-        res = solve()
+        block()
     sampler = ClockSampler(device)
     sampler.start()
     dist.barrier()
-    S.reset()  # counters and event times cleared; the timed solves follow
-    t_dev = 0.0
+    t_before = S.timing()
+    sampler.begin()
     t_wall0 = time.perf_counter()
-    step_ms = plain_ms = 0.0
-    plain_launches = launches = kernels = 0
     for _ in range(a.steps):
-        S.reset()
-        S.run()
-        res = S.evaluate()
-        t = S.timing()
-        t_dev += t["run_ms"] + t["eval_ms"]
-        step_ms += t["step_ms"]
-        plain_ms += t["step_ms_plain"]
-        plain_launches += t["step_launches_plain"]
-        launches += t["step_launches"]
-        kernels += t["kernel_launches"]
+        block()
     wall = time.perf_counter() - t_wall0
+    sampler.end()
     dist.barrier()
-    clocks = sampler.stop()
-    t_dev_max = dist.max(t_dev)
-    units = dist.sum(NF * run["steps"] * a.steps)
+    t_after = S.timing()
+    d = {k: t_after[k] - t_before[k] for k in t_after}
+    t_dev_max = dist.max(d["step_ms"])
+    units = dist.sum(NF * a.block * a.steps)
     value = units / (t_dev_max * 1e-3) / 1e6
     ms_per_step = t_dev_max / a.steps
 
-    # end to end through the C ABI with host buffers
-    e2e_times, h2d, d2h = [], 0, 0
-    e2e_kernels = 0
-    for i in range(a.warmup + a.steps):
+    # end to end through the C ABI with host buffers: whole solves from host triangles
+    e2e_times, h2d, d2h, e2e_kernels, kpis = [], 0, 0, 0, None
+    for i in range(a.e2e_solves):
+        sampler.begin()
         t0 = time.perf_counter()
         g2 = E.prepare({"tris": tris, **p})
         S2 = E.Simulation(g2, runp)
         S2.run()
         r2 = S2.evaluate()
         el = time.perf_counter() - t0
-        if i >= a.warmup:
-            e2e_times.append(el)
-            gi, t2 = g2.info, S2.timing()
-            h2d = gi.h2d_bytes + t2["h2d_bytes"]
-            d2h = gi.d2h_bytes + t2["d2h_bytes"]
-            e2e_kernels = gi.kernel_launches + t2["kernel_launches"]
+        sampler.end()
+        e2e_times.append(el)
+        gi, t2 = g2.info, S2.timing()
+        h2d = gi.h2d_bytes + t2["h2d_bytes"]
+        d2h = gi.d2h_bytes + t2["d2h_bytes"]
+        e2e_kernels = gi.kernel_launches + t2["kernel_launches"]
+        kpis = r2["metrics"]
         del S2, g2
+    clocks = sampler.stop()
     e2e_t = dist.max(sum(e2e_times)) / len(e2e_times)
     e2e = dist.sum(NF * run["steps"]) / e2e_t / 1e6
 
-    # the reference's whole evaluate() result object (cut planes, field3d, streamlines) on top of the KPIs
-    E.evaluate(S)
-    t0 = time.perf_counter()
-    E.evaluate(S)
-    evaluate_full_ms = (time.perf_counter() - t0) * 1e3
-
     # roofline of the fused step kernel (launches without averaging)
     bytes_per_cell = 2 * 19 * (4 if a.storage == "f32" else 2)
-    avg_launch_ms = plain_ms / max(plain_launches, 1)
+    avg_launch_ms = d["step_ms_plain"] / max(d["step_launches_plain"], 1)
     achieved = bytes_per_cell * NF / (avg_launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
     traffic = ncu_traffic(f"lbm_step_{a.storage}_{a.workload}")
@@ -628,25 +708,22 @@ def main():
                 "frac": round(achieved / peak, 4), "traffic": traffic,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "kernel": f"aa_step_kernel<{a.storage}> (fused pull-stream+collide, A-A in place)",
-                "bytes_per_launch": bytes_per_cell * NF, "avg_launch_us": round(avg_launch_ms * 1e3, 3)}
+                "bytes_per_launch": bytes_per_cell * NF, "avg_launch_us": round(avg_launch_ms * 1e3, 3),
+                "launches_timed": int(d["step_launches_plain"])}
 
     line = {"metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": ws, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": a.storage, "data": "synthetic",
-            "config": {"workload": desc, "grid": [g.nx, g.ny, g.nz], "NF": NF, "lbm_steps_per_bench_step": run["steps"],
-                       "averaged_steps": run["avg"], "storage": a.storage,
-                       "state_bytes": int(S.info.state_bytes),
-                       "l2": "state larger than the 129 MB L2, no flush needed" if S.info.state_bytes > 129e6
-                       else "state smaller than L2",
-                       "parallelism": f"replicas x{ws}"},
-            "kpis": {k: round(res["metrics"][k], 6) for k in ("gamma", "gammaCore", "lowCore", "maxToMean", "zeta")},
+            "config": bench_config(desc, (g.nx, g.ny, g.nz), NF, run, a.block, a.storage, ws),
+            "device_state_bytes": int(S.info.state_bytes),
+            "kpis_e2e_solve": {k: round(kpis[k], 6) for k in ("gamma", "gammaCore", "lowCore", "maxToMean", "zeta")},
             "e2e": {"value": round(e2e, 1), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_t * 1e3, 3)},
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_t * 1e3, 3),
+                    "step": f"one whole solve ({run['steps']} LBM steps), {a.e2e_solves} timed"},
             "roofline": roofline,
-            "gpu_launches": int(kernels),
+            "gpu_launches": int(d["kernel_launches"]),
             "gpu_launches_e2e_per_step": int(e2e_kernels),
-            "evaluate_full_result_ms": round(evaluate_full_ms, 2),
-            "wall_s_timed": round(wall, 3),
+            "wall_s_timed": round(wall + sum(e2e_times), 3),
             "clocks": clocks}
     if rank == 0 and not a.no_cpu_baseline:
         v, n, el, nf = cpu_baseline(spec, run, 1)

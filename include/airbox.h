@@ -24,8 +24,9 @@ extern "C" {
 #endif
 
 /* Version of the structures and entry points below; a host compares it with abx_abi_version() before use.
- * 2: prepare timings in abx_geom_info, coordinate channels in abx_net_params, batch groups. */
-#define ABX_ABI_VERSION 2
+ * 2: prepare timings in abx_geom_info, coordinate channels in abx_net_params, batch groups.
+ * 3: abx_run_params.flags (bfloat16 storage only on request). */
+#define ABX_ABI_VERSION 3
 
 /* Status codes.  The first group mirrors the errors engine.js throws. */
 typedef enum {
@@ -52,7 +53,10 @@ typedef enum {
   ABX_STORE_F32 = 0,        /* float32 populations, float32 collision (the WGSL lbm_step contract, src/engine.js:378-450) */
   ABX_STORE_F32_EXACT = 1,  /* float32 populations, float64 collision in cpuStep's exact operation order (src/engine.js:266-321) */
   ABX_STORE_F16 = 2,        /* binary16 shifted deviations f - w_i, float32 collision */
-  ABX_STORE_BF16 = 3,       /* bfloat16 shifted deviations f - w_i, float32 collision */
+  ABX_STORE_BF16 = 3,       /* bfloat16 shifted deviations f - w_i, float32 collision; only with
+                               ABX_RUN_ALLOW_BF16: its 8 significant bits do not resolve the density
+                               differences behind zeta on large, fine grids (6.5 % off the float64 run
+                               on a 512x256x384-cell airbox, where float16 stays within 0.5 %) */
   ABX_STORE_F64 = 4         /* float64 populations and collision (an FP64 run on the GPU) */
 } abx_storage;
 
@@ -116,11 +120,15 @@ int abx_geom_get_masks(const abx_geom *g, uint8_t *solid, uint8_t *fluid, uint8_
  * recomputed on the GPU on demand.  For grids up to 2^31 fine voxels. */
 int abx_geom_get_fine(const abx_geom *g, uint8_t *fine, size_t cap);
 
+/* abx_run_params.flags */
+#define ABX_RUN_ALLOW_BF16 1u    /* accept ABX_STORE_BF16 (rejected otherwise: its KPIs can miss 0.5 %) */
+
 /* simulate() parameters (src/engine.js:237, fields of src/ui.html:502-504). */
 typedef struct {
   double K, aniso, u, tau;       /* filter resistance, cross-pleat factor, inlet speed, relaxation time */
   int steps, avg, every;         /* time steps, averaged tail, progress interval */
   int storage;                   /* abx_storage */
+  unsigned flags;                /* ABX_RUN_* bits; 0 for the reference's behaviour */
 } abx_run_params;
 
 typedef struct abx_sim abx_sim;
@@ -265,7 +273,12 @@ int abx_sim_get_timing(const abx_sim *s, abx_sim_timing *out);
  * scratch are rejected with ABX_ERR_INVALID_ARGUMENT and a message giving the
  * size.  The first call on a device looks up that array's device address
  * (cudaGetSymbolAddress, with the device current); make that first call
- * before any stream capture.  All calls share the one array and it keeps the
+ * before any stream capture.  The address is looked up again when the
+ * device's context has changed since (after a cudaDeviceReset the library
+ * is loaded anew at another address) and after a call that failed with a
+ * CUDA error; such a call, too, should come before any stream capture.
+ * The call makes the current device's primary context current (cudaSetDevice).
+ * All calls share the one array and it keeps the
  * previous call's contents, so calls that overlap on the GPU (other streams,
  * other threads) race: issue them one after another.  stream may be NULL. */
 int abx_voxelize_static(const float *d_tris, size_t nfloats, const double origin[3], double h, int nx, int ny, int nz,

@@ -1,6 +1,7 @@
 """Generate the golden fixtures in tests/golden/ by running the reference's own
 Python CLI, airbox_cfd.py (Awsmqt/AirboxCalc), imported from the reference
-checkout given by --reference (default: /root/reference).
+checkout given by --reference or by the AIRBOXCALC_REFERENCE environment variable
+(one of the two is required).
 
 The reference ships no tests, fixtures or STL files.  What its Python code can
 pin for the compute core:
@@ -25,7 +26,8 @@ geometries use dimensions that are not multiples of the cell size.  main()
 imports matplotlib only in report(); a stand-in module is installed for that
 call (matplotlib is not installed here).
 
-Run:  python tests/golden/make_golden.py [--reference PATH]
+Run:  python tests/golden/make_golden.py --reference PATH
+      (or AIRBOXCALC_REFERENCE=PATH python tests/golden/make_golden.py)
 """
 from __future__ import annotations
 
@@ -96,8 +98,11 @@ def run_main(R, stl_path, spec: ag.AirboxSpec, workdir, steps=1, avg=1):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("AIRBOXCALC_REFERENCE"),
+                    help="checkout of the reference holding airbox_cfd.py (default: $AIRBOXCALC_REFERENCE)")
     a = ap.parse_args()
+    if not a.reference:
+        ap.error("give the reference checkout with --reference PATH or AIRBOXCALC_REFERENCE")
     sys.dont_write_bytecode = True   # leave the reference checkout untouched
     sys.path.insert(0, a.reference)
     import airbox_cfd as R  # the reference's own module

@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol():
     L = A.load()
     for name in header_symbols():
         assert hasattr(L, name), name
-    assert L.abx_abi_version() == 2
+    assert L.abx_abi_version() == A.ABI_VERSION == 3
 
 
 @pytest.mark.parametrize("key", ["stl_binary", "stl_ascii"])

@@ -34,7 +34,7 @@ def individual(g, p):
 @pytest.mark.parametrize("tuned", [False, True])
 def test_batch_matches_individual_runs(storage, tuned):
     geoms, params = variants()
-    params = [dict(p, storage=storage) for p in params]
+    params = [dict(p, storage=storage, allowBf16=True) for p in params]
     B = BT.Batch(geoms, params)
     if tuned:
         t = B.tune()

@@ -167,7 +167,7 @@ def test_reference_self_test(storage, tol):
     md = 0.0
     for ns in (None, bulk_ns(So, So.NF)):
         f = oracle_steps(So, So.f0(), 12, "f32", ns)
-        Sg = E.Simulation(g, {**RUN, "storage": storage}, ns=ns)
+        Sg = E.Simulation(g, {**RUN, "storage": storage, "allowBf16": True}, ns=ns)
         Sg.step(12)
         d = np.abs(Sg.get_f() - f)[::7]
         md = max(md, float(d.max()))
@@ -181,7 +181,7 @@ def run_both(spec, storage, steps, avg, every, extra_run=None):
     So = O.OracleSim(og, run)
     acc_o, hist_o = So.simulate(steps, avg, every, nthreads=NT)
     m_o, fmap_o = So.evaluate(acc_o)
-    Sg = E.Simulation(g, {**run, "storage": storage})
+    Sg = E.Simulation(g, {**run, "storage": storage, "allowBf16": True})
     Sg.run()
     res = Sg.evaluate()
     return So, Sg, acc_o, hist_o, m_o, fmap_o, res
@@ -261,7 +261,7 @@ def test_tma_pipeline_matches_direct_kernel(storage, monkeypatch):
         else:
             monkeypatch.delenv("ABX_TMA", raising=False)
         for with_ns in (False, True):
-            S = E.Simulation(g, {**RUN, "storage": storage}, ns=ns if with_ns else None)
+            S = E.Simulation(g, {**RUN, "storage": storage, "allowBf16": True}, ns=ns if with_ns else None)
             assert S.info.tma_pipeline == (1 if tma else 0)
             S.step(7)
             S.step(6, accumulate=True)
@@ -282,7 +282,7 @@ def test_zero_inflow_fails_like_the_reference(storage):
     with pytest.raises(O.OracleError) as eo:
         O.OracleSim(og, run).simulate(200, 50, 50, nthreads=NT)
     with pytest.raises(E.AirboxError) as eg:
-        E.Simulation(g, {**run, "storage": storage}).run()
+        E.Simulation(g, {**run, "storage": storage, "allowBf16": True}).run()
     assert eg.value.code == 10 and str(eg.value) == str(eo.value)
 
 
@@ -296,7 +296,7 @@ def test_instability_reported_like_the_reference(storage):
     So = O.OracleSim(og, run)
     with pytest.raises(O.OracleError) as eo:
         So.simulate(3000, 100, 50, nthreads=NT)
-    S = E.Simulation(g, {**run, "storage": storage})
+    S = E.Simulation(g, {**run, "storage": storage, "allowBf16": True})
     with pytest.raises(E.AirboxError) as eg:
         S.run()
     assert eg.value.code == 10 and "Rechnung instabil bei Schritt" in str(eg.value)

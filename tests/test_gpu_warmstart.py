@@ -112,7 +112,7 @@ def test_warm_start_populations_match_restatement(storage, tol):
     w = net.get_weights()
     w[-(4 * 8 * 27 + 4):] *= 20.0
     net.set_weights(w)
-    S = E.Simulation(g, dict(RUN, storage=storage))
+    S = E.Simulation(g, dict(RUN, storage=storage, allowBf16=True))
     feats, pred = net.predict(S)
     W.warm_start(S, net)
     f = S.get_f().reshape(19, -1)
