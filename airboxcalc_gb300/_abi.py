@@ -72,7 +72,8 @@ class SimInfo(C.Structure):
     _fields_ = [("NF", C.c_int), ("Ain", C.c_int), ("Af", C.c_int), ("Lp", C.c_int), ("n_layer_m", C.c_int),
                 ("n_layer_t", C.c_int), ("u0", C.c_double), ("tau0", C.c_double), ("sig", C.c_double),
                 ("aniso", C.c_double), ("cs2s", C.c_double), ("uface", C.c_double), ("step", C.c_int),
-                ("nacc", C.c_int), ("Np", C.c_int64), ("state_bytes", C.c_int64), ("tma_pipeline", C.c_int)]
+                ("nacc", C.c_int), ("Np", C.c_int64), ("state_bytes", C.c_int64), ("tma_pipeline", C.c_int),
+                ("vec_width", C.c_int), ("vec_interior_cells", C.c_int64)]
 
 
 class Progress(C.Structure):

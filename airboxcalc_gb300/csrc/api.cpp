@@ -157,10 +157,18 @@ struct abx_geom {
   int Ain = 0, Lp = 0;
   int64_t launches = 0, h2d = 0, d2h = 0;
   double ms_vox = 0, ms_masks = 0, ms_device = 0;
+  // work lists of the vectorised step kernel, per block width V = 2, 4, 8 (built on first use)
+  struct VecLists {
+    bool ready = false;
+    uint32_t *d_blk = nullptr;
+    uint2 *d_bseg = nullptr;
+    uint32_t n_bulk = 0, n_filter = 0, nbseg = 0;
+  } vec[3];
   ~abx_geom() {
     cudaSetDevice(device);
     cudaFree(d_solid); cudaFree(d_fluid); cudaFree(d_outlet);
     cudaFree(d_mask); cudaFree(d_seg); cudaFree(d_opening); cudaFree(d_cells);
+    for (auto &v : vec) { cudaFree(v.d_blk); cudaFree(v.d_bseg); }
   }
 };
 
@@ -683,6 +691,9 @@ struct abx_sim {
   double u0 = 0, tau0 = 0, sig = 0, aniso = 0, cs2s = 0, uface = 0;
   bool has_ns = false;
   TmaBlob tma;               // tensor maps of the TMA-pipelined step kernel (tma.ready when in use)
+  int vec_V = 0;             // block width of the vectorised step kernel (0: the one-cell-per-lane kernel)
+  bool va_ready = false;
+  VecArgs va{};              // its work lists (the geometry's)
   bool use_graphs = true;    // ABX_NO_GRAPH=1 launches the step kernels one by one
   std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
   bool timing = false;
@@ -741,6 +752,49 @@ static int sim_reset(abx_sim *s) {
   s->launches = 1; s->h2d = 0; s->d2h = 0;
   s->ev_used = 0; s->ev_kind.clear(); s->ev_nsteps.clear();
   return ABX_OK;
+}
+
+static int vec_index(int V) { return V == 2 ? 0 : V == 4 ? 1 : V == 8 ? 2 : -1; }
+
+// The geometry's interior-block and boundary-segment lists for block width V (built once, kept on the device).
+static int geom_vec_lists(abx_geom &g, int V, cudaStream_t st) {
+  const int vi = vec_index(V);
+  if (vi < 0) return fail(ABX_ERR_INVALID_ARGUMENT, "vector lists: block width %d", V);
+  abx_geom::VecLists &L = g.vec[vi];
+  if (L.ready) return ABX_OK;
+  CK(cudaSetDevice(g.device), "vector lists: set device");
+  const int64_t items = (int64_t)g.nseg * (32 / V);
+  const int64_t nb = prep_compact_blocks(std::max<int64_t>(items, 1));
+  DevBuf dbc, doff, dcnt;
+  CK(cudaMalloc(&dbc.p, sizeof(uint32_t) * std::max<int64_t>(nb, 1)), "vector lists");
+  CK(cudaMalloc(&doff.p, sizeof(unsigned long long) * (nb + 1)), "vector lists");
+  CK(cudaMalloc(&dcnt.p, 3 * sizeof(unsigned long long)), "vector lists");
+  CK(prep_vec_lists(g.d_seg, g.nseg, g.d_mask, V, nullptr, nullptr, (uint32_t *)dbc.p, (unsigned long long *)doff.p,
+                    (unsigned long long *)dcnt.p, st), "vector lists: count");
+  unsigned long long c[3];
+  CK(cudaMemcpyAsync(c, dcnt.p, sizeof c, cudaMemcpyDeviceToHost, st), "vector lists");
+  CK(cudaStreamSynchronize(st), "vector lists");
+  CK(cudaMalloc((void **)&L.d_blk, sizeof(uint32_t) * std::max<unsigned long long>(c[0] + c[1], 1)), "vector lists");
+  CK(cudaMalloc((void **)&L.d_bseg, sizeof(uint2) * std::max<unsigned long long>(c[2], 1)), "vector lists");
+  CK(prep_vec_lists(g.d_seg, g.nseg, g.d_mask, V, L.d_blk, L.d_bseg, (uint32_t *)dbc.p, (unsigned long long *)doff.p,
+                    (unsigned long long *)dcnt.p, st), "vector lists: write");
+  CK(cudaStreamSynchronize(st), "vector lists");
+  L.n_bulk = (uint32_t)c[0]; L.n_filter = (uint32_t)c[1]; L.nbseg = (uint32_t)c[2];
+  L.ready = true;
+  return ABX_OK;
+}
+
+// Block width of the vectorised step kernel for a storage (ABX_VEC=0: the one-cell-per-lane kernel everywhere;
+// ABX_VEC_V=n: that width where the storage has it).
+static int vec_width(int storage) {
+  if (const char *e = std::getenv("ABX_VEC")) if (e[0] == '0') return 0;
+  int want = 0;
+  if (const char *e = std::getenv("ABX_VEC_V")) want = std::atoi(e);
+  switch (storage) {
+    case ABX_STORE_F32: return (want == 2 || want == 4) ? want : 2;
+    case ABX_STORE_F16: case ABX_STORE_BF16: return (want == 2 || want == 4) ? want : 4;
+  }
+  return 0;
 }
 
 extern "C" int abx_sim_create(abx_geom *g, const abx_run_params *p, const float *ns, abx_sim **out) {
@@ -808,6 +862,9 @@ extern "C" int abx_sim_create(abx_geom *g, const abx_run_params *p, const float 
     if (te != cudaSuccess && te != cudaErrorNotSupported) return cuda_fail(te, "sim_create: tensor maps");
     cudaGetLastError();
   }
+  // the vectorised step kernel (not with a partial bounce-back field, nor next to the opt-in TMA kernel); its
+  // work lists are built before the first step
+  if (!ns && !s.tma.ready) s.vec_V = vec_width(p->storage);
   int rc = sim_reset(&s);
   if (rc) return rc;
   s.h2d = create_h2d;
@@ -826,6 +883,8 @@ extern "C" int abx_sim_get_info(const abx_sim *s, abx_sim_info *o) {
   o->step = s->step; o->nacc = s->nacc; o->Np = s->g->Np;
   o->state_bytes = (int64_t)(store_bytes(s->p.storage) * 19 + acc_bytes(s->p.storage) * 4) * s->g->Np;
   o->tma_pipeline = s->tma.ready ? 1 : 0;
+  o->vec_width = s->vec_V;
+  o->vec_interior_cells = s->va_ready ? (int64_t)(s->va.n_bulk + s->va.n_filter) * s->vec_V : 0;
   return ABX_OK;
 }
 
@@ -848,6 +907,13 @@ static cudaEvent_t next_event(abx_sim *s) {
 // in "out" form), as one CUDA graph per (n, form, accumulate).
 static int run_steps(abx_sim *s, int n, bool acc) {
   if (n <= 0) return ABX_OK;
+  if (s->vec_V && !s->va_ready) {
+    if (int rc = geom_vec_lists(*s->g, s->vec_V, s->st)) return rc;
+    const abx_geom::VecLists &L = s->g->vec[vec_index(s->vec_V)];
+    s->va.blk = L.d_blk; s->va.n_bulk = L.n_bulk; s->va.n_filter = L.n_filter;
+    s->va.bseg = L.d_bseg; s->va.nbseg = L.nbseg;
+    s->va_ready = true;
+  }
   if (!s->use_graphs) {
     const StepArgs a = step_args(*s);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -856,7 +922,9 @@ static int run_steps(abx_sim *s, int n, bool acc) {
       if (e0 && e1) { cudaEventRecord(e0, s->st); s->ev_kind.push_back(acc ? 1 : 0); s->ev_nsteps.push_back(n); }
     }
     for (int i = 0; i < n; i++) {
-      CK(launch_step(s->p.storage, s->form == 0, acc, s->has_ns, a, s->tma.ready ? &s->tma : nullptr, s->st), "run: step");
+      CK(s->vec_V ? launch_step_vec(s->p.storage, s->vec_V, s->form == 0, acc, a, s->va, s->st)
+                  : launch_step(s->p.storage, s->form == 0, acc, s->has_ns, a, s->tma.ready ? &s->tma : nullptr, s->st),
+         "run: step");
       s->form ^= 1;
     }
     if (e0 && e1) cudaEventRecord(e1, s->st);
@@ -877,7 +945,8 @@ static int run_steps(abx_sim *s, int n, bool acc) {
     cudaError_t le = cudaSuccess;
     int form = s->form;
     for (int i = 0; i < n && le == cudaSuccess; i++) {
-      le = launch_step(s->p.storage, form == 0, acc, s->has_ns, a, s->tma.ready ? &s->tma : nullptr, s->st);
+      le = s->vec_V ? launch_step_vec(s->p.storage, s->vec_V, form == 0, acc, a, s->va, s->st)
+                    : launch_step(s->p.storage, form == 0, acc, s->has_ns, a, s->tma.ready ? &s->tma : nullptr, s->st);
       form ^= 1;
     }
     cudaError_t ce = cudaStreamEndCapture(s->st, &graph);

@@ -40,6 +40,15 @@ __host__ __device__ __forceinline__ uint32_t seg_base(uint2 s) { return s.x & ~k
 // Storage formats of the populations.  Shifted formats hold f - w_q.
 enum StoreKind { kStoreF32 = 0, kStoreF32Exact = 1, kStoreF16 = 2, kStoreBF16 = 3, kStoreF64 = 4 };
 
+// Reciprocal and square root of collide_fast: correctly rounded, or (FAST) the hardware approximations
+// (rcp.approx / sqrt.approx: about one unit in the last place, one MUFU instruction instead of an iteration
+// with a special-case branch).  The 16-bit storages take FAST (ABX_FAST_MATH16, default 1): their kernels are
+// short of issue slots and their stored values carry 11 or 8 significant bits (config2 float16 step 38.8 ->
+// 37.0 us); the float32 kernels keep the correctly rounded forms (no gain there: config3 1038 vs 1049 us).
+#ifndef ABX_FAST_MATH16
+#define ABX_FAST_MATH16 1
+#endif
+
 template <int K> struct Store;
 // Cache hints for the float32 populations.  A population written by a step is read only by the next step,
 // so stores are marked evict-first; loads stay default: the odd step's neighbour pulls read each line from
@@ -52,9 +61,16 @@ template <int K> struct Store;
 // ld/st address global memory; lds reads a value staged in shared memory.
 // Every format also has raw accessors (ldr / ldsr / str) that the step kernels use: the stored value itself,
 // i.e. f for the plain formats and h = f - w_q for the shifted ones (whose collision then works on h).
+// Collision convention of every format: kCollideShifted - the float32 collision works on h = f - w_q (toc maps a
+// stored value to it, fromc back); kFastMath - approximate reciprocal and square root in that collision.
+// float32 storage keeps f itself but collides on h: the density and stress sums of values near w_q then keep
+// the small deviations that carry rho - 1 (colliding on f loses them to the rounding of sums near 1: on a
+// 512x256x384-cell airbox the time-averaged rho - 1 came out 1.9e-3 (relative L2) off the float64 run, against
+// 1e-5 with cpuStep's float64 arithmetic on the same float32 storage).
 template <> struct Store<kStoreF32> {
   using T = float; using L = float; using Acc = float;
   static constexpr bool kShifted = false;
+  static constexpr bool kCollideShifted = true, kFastMath = false;
   __device__ static __forceinline__ L lds(const T *p, L) { return *p; }
   __device__ static __forceinline__ L ldsr(const T *p) { return *p; }
 #if ABX_CACHE_HINTS == 2
@@ -73,6 +89,7 @@ template <> struct Store<kStoreF32> {
 template <> struct Store<kStoreF32Exact> {
   using T = float; using L = double; using Acc = float;
   static constexpr bool kShifted = false;
+  static constexpr bool kCollideShifted = false, kFastMath = false;
   __device__ static __forceinline__ L lds(const T *p, L) { return (L)*p; }
   __device__ static __forceinline__ L ld(const T *p, L) { return (L)*p; }
   __device__ static __forceinline__ void st(T *p, L v, L) { *p = (float)v; }
@@ -83,6 +100,7 @@ template <> struct Store<kStoreF32Exact> {
 template <> struct Store<kStoreF16> {
   using T = __half; using L = float; using Acc = float;
   static constexpr bool kShifted = true;
+  static constexpr bool kCollideShifted = true, kFastMath = ABX_FAST_MATH16;
   __device__ static __forceinline__ L lds(const T *p, L w) { return w + __half2float(*p); }
   __device__ static __forceinline__ L ld(const T *p, L w) { return w + __half2float(*p); }
   __device__ static __forceinline__ void st(T *p, L v, L w) { *p = __float2half_rn(v - w); }
@@ -93,6 +111,7 @@ template <> struct Store<kStoreF16> {
 template <> struct Store<kStoreBF16> {
   using T = __nv_bfloat16; using L = float; using Acc = float;
   static constexpr bool kShifted = true;
+  static constexpr bool kCollideShifted = true, kFastMath = ABX_FAST_MATH16;
   __device__ static __forceinline__ L lds(const T *p, L w) { return w + __bfloat162float(*p); }
   __device__ static __forceinline__ L ld(const T *p, L w) { return w + __bfloat162float(*p); }
   __device__ static __forceinline__ void st(T *p, L v, L w) { *p = __float2bfloat16_rn(v - w); }
@@ -103,6 +122,7 @@ template <> struct Store<kStoreBF16> {
 template <> struct Store<kStoreF64> {
   using T = double; using L = double; using Acc = double;
   static constexpr bool kShifted = false;
+  static constexpr bool kCollideShifted = false, kFastMath = false;
   __device__ static __forceinline__ L lds(const T *p, L) { return *p; }
   __device__ static __forceinline__ L ld(const T *p, L) { return *p; }
   __device__ static __forceinline__ void st(T *p, L v, L) { *p = v; }
@@ -113,6 +133,16 @@ template <> struct Store<kStoreF64> {
 
 template <class L> __device__ __forceinline__ L weight(int q) {
   return wclass(q) == 0 ? (L)1 / (L)3 : (wclass(q) == 1 ? (L)1 / (L)18 : (L)1 / (L)36);
+}
+
+// Stored value of direction q -> the value the collision works on, and back (see kCollideShifted).
+template <int K, class L> __device__ __forceinline__ L toc(L raw, int q) {
+  if constexpr (Store<K>::kCollideShifted && !Store<K>::kShifted) return raw - weight<L>(q);
+  else return raw;
+}
+template <int K, class L> __device__ __forceinline__ L fromc(L v, int q) {
+  if constexpr (Store<K>::kCollideShifted && !Store<K>::kShifted) return v + weight<L>(q);
+  else return v;
 }
 
 // c_q . u with the zero components left out: exactly the value of
@@ -213,14 +243,6 @@ __device__ __forceinline__ void collide(const L (&fi)[19], uint32_t cls, L nsv, 
   }
 }
 
-// Reciprocal and square root of collide_fast: correctly rounded, or (FAST) the hardware approximations
-// (rcp.approx / sqrt.approx: about one unit in the last place, one MUFU instruction instead of an iteration
-// with a special-case branch).  The 16-bit storages take FAST (ABX_FAST_MATH16, default 1): their kernels are
-// short of issue slots and their stored values carry 11 or 8 significant bits (config2 float16 step 38.8 ->
-// 37.0 us); the float32 kernels keep the correctly rounded forms (no gain there: config3 1038 vs 1049 us).
-#ifndef ABX_FAST_MATH16
-#define ABX_FAST_MATH16 1
-#endif
 template <bool FAST> __device__ __forceinline__ float cf_rcp(float x) {
   if constexpr (FAST) {
     float y;
@@ -247,7 +269,7 @@ template <bool FAST> __device__ __forceinline__ float cf_sqrt(float x) {
 // exactly rho/3 I + rho u u on D3Q19), and equilibrium plus BGK per opposite
 // pair from a shared even part and an odd part.  Same model as collide();
 // about a third of its arithmetic.
-template <bool HAS_NS, bool SHIFTED = false>
+template <bool HAS_NS, bool SHIFTED = false, bool FAST = false>
 __device__ __forceinline__ void collide_fast(const float (&f)[19], uint32_t cls, float nsv_in,
                                              const CollideParams<float> &P, float (&fo)[19], float &ux, float &uy,
                                              float &uz, float &rho) {
@@ -272,7 +294,6 @@ __device__ __forceinline__ void collide_fast(const float (&f)[19], uint32_t cls,
   const float jx = d1 + (d7 + d9) + (d11 + d13);
   const float jy = d3 + (d7 - d9) + (d15 + d17);
   const float jz = d5 + (d11 - d13) + (d15 - d17);
-  constexpr bool FAST = SHIFTED && ABX_FAST_MATH16;
   const float inv = cf_rcp<FAST>(rho);
   ux = jx * inv; uy = jy * inv; uz = jz * inv;
   float vx = ux, vy = uy, vz = uz;   // velocity of the equilibrium

@@ -5,6 +5,7 @@
 // tensor maps could be made, and the direct-load kernel (lbm_kernels.cuh).
 #include "lbm_kernels.cuh"
 #include "lbm_tma.cuh"
+#include "lbm_vec.cuh"
 
 #include <cudaTypedefs.h>
 
@@ -23,10 +24,11 @@ namespace abx {
 #define ABX_PDL 1
 #endif
 template <class... KArgs, class... Args>
-static cudaError_t launch_step_kernel(void (*kern)(KArgs...), unsigned grid, cudaStream_t st, Args &&...args) {
+static cudaError_t launch_step_kernel_t(void (*kern)(KArgs...), unsigned grid, unsigned threads, cudaStream_t st,
+                                       Args &&...args) {
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(256);
+  cfg.blockDim = dim3(threads);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = st;
   cudaLaunchAttribute at[1];
@@ -35,6 +37,10 @@ static cudaError_t launch_step_kernel(void (*kern)(KArgs...), unsigned grid, cud
   cfg.attrs = at;
   cfg.numAttrs = ABX_PDL ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+template <class... KArgs, class... Args>
+static cudaError_t launch_step_kernel(void (*kern)(KArgs...), unsigned grid, cudaStream_t st, Args &&...args) {
+  return launch_step_kernel_t(kern, grid, 256, st, std::forward<Args>(args)...);
 }
 
 template <int K>
@@ -51,6 +57,48 @@ static cudaError_t step_k(bool odd, bool acc, bool has_ns, const StepArgs &a, cu
   }
 #undef ABX_L
   return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ vectorised step (V cells per thread)
+template <int K, int V>
+static cudaError_t step_vec_k(bool odd, bool acc, const StepArgs &a, const VecArgs &v, cudaStream_t st) {
+  const uint32_t items = (v.n_bulk + 31u) / 32u + (v.n_filter + 31u) / 32u + v.nbseg;
+  if (items == 0) return cudaSuccess;
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm <= 0) nsm = 1;
+  }
+  constexpr unsigned T = VecShape<K, V>::kThreads, W = T / 32;
+  const unsigned need = (items + W - 1) / W, res = (unsigned)nsm * VecShape<K, V>::kMinBlocks;
+  const unsigned grid = need < res ? need : res;
+  if (odd) {
+    if (acc) return launch_step_kernel_t(aa_vec_kernel<K, V, true, true>, grid, T, st, a, v);
+    return launch_step_kernel_t(aa_vec_kernel<K, V, true, false>, grid, T, st, a, v);
+  }
+  if (acc) return launch_step_kernel_t(aa_vec_kernel<K, V, false, true>, grid, T, st, a, v);
+  return launch_step_kernel_t(aa_vec_kernel<K, V, false, false>, grid, T, st, a, v);
+}
+
+cudaError_t launch_step_vec(int storage, int V, bool odd, bool acc, const StepArgs &a, const VecArgs &v,
+                            cudaStream_t st) {
+  switch (storage) {
+    case kStoreF32:
+      if (V == 4) return step_vec_k<kStoreF32, 4>(odd, acc, a, v, st);
+      if (V == 2) return step_vec_k<kStoreF32, 2>(odd, acc, a, v, st);
+      break;
+    case kStoreF16:
+      if (V == 4) return step_vec_k<kStoreF16, 4>(odd, acc, a, v, st);
+      if (V == 2) return step_vec_k<kStoreF16, 2>(odd, acc, a, v, st);
+      break;
+    case kStoreBF16:
+      if (V == 4) return step_vec_k<kStoreBF16, 4>(odd, acc, a, v, st);
+      if (V == 2) return step_vec_k<kStoreBF16, 2>(odd, acc, a, v, st);
+      break;
+  }
+  return cudaErrorInvalidValue;
 }
 
 // ------------------------------------------------------------------ batched step (many domains)

@@ -75,6 +75,26 @@ struct alignas(64) TmaBlob {
 cudaError_t make_tma(int storage, const StepArgs &a, TmaBlob *out);
 void free_tma(TmaBlob *b);
 
+// Work lists of the vectorised step kernel (lbm_vec.cuh), built per geometry and block width V (cells per
+// thread, consecutive along k): interior blocks - V fluid cells whose 18 pull neighbours are all fluid, all of
+// class bulk or all of class filter - and the remaining fluid cells as boundary segments.
+struct VecArgs {
+  const uint32_t *blk;     // padded index of the first cell of every interior block: bulk blocks, then filter blocks
+  uint32_t n_bulk, n_filter;
+  const uint2 *bseg;       // boundary segments {base | kSegInterior flag, lane mask of their cells}
+  uint32_t nbseg;
+};
+// The lists of a geometry for block width V (4 or 8): call with blk == bseg == nullptr to get the three
+// counts (counts[0..2] = bulk blocks, filter blocks, boundary segments), then with arrays of those sizes.
+// block_counts / offsets: scratch of prep_compact_blocks(nseg * 32 / V) and + 1 entries.
+cudaError_t prep_vec_lists(const uint2 *seg, uint32_t nseg, const uint32_t *mask, int V, uint32_t *blk, uint2 *bseg,
+                           uint32_t *block_counts, unsigned long long *offsets, unsigned long long *counts,
+                           cudaStream_t st);
+// One step through the vectorised kernel (lbm_fast.cu; float32 with V = 4, float16 / bfloat16 with V = 4 or 8;
+// no partial bounce-back field).
+cudaError_t launch_step_vec(int storage, int V, bool odd, bool acc, const StepArgs &a, const VecArgs &v,
+                            cudaStream_t st);
+
 // Launchers (defined in lbm_fast.cu / lbm_exact.cu).  storage: abx_storage
 // value; tma (may be null) selects the TMA-pipelined kernel.
 cudaError_t launch_step(int storage, bool odd, bool acc, bool has_ns, const StepArgs &a, const TmaBlob *tma,

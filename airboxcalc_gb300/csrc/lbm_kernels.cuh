@@ -54,20 +54,13 @@ template <class L> __device__ __forceinline__ CollideParams<L> make_params(const
 #endif
 constexpr int kStepSpw = ABX_STEP_SPW;
 
-// One warp's share of a step: SPW segments starting at s0 of the domain described by `a`.
+// One warp's share of a step: the fluid cells (lane masks) of SPW segments {base | flag, lane mask}.
 template <int K, bool ODD, bool ACC, bool HAS_NS, int SPW, class Args>
-__device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, const uint32_t lane) {
+__device__ __forceinline__ void step_cells(const Args &a, const uint2 (&sg)[SPW], const uint32_t lane) {
   using S = Store<K>;
   using T = typename S::T;
   using L = typename S::L;
   using Acc = typename S::Acc;
-  if (s0 >= a.nseg) return;
-  // the run-state word changes only between launches: a plain load issued together with the segment's
-  const int halted = a.status ? *a.status : 0;
-  uint2 sg[SPW];
-#pragma unroll
-  for (int j = 0; j < SPW; j++) sg[j] = (s0 + j < a.nseg) ? a.seg[s0 + j] : make_uint2(0, 0);
-  if (halted) return;
   T *f = (T *)a.f;
   const uint32_t Np = (uint32_t)a.Np;
   bool act[SPW];
@@ -90,10 +83,10 @@ __device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, cons
       // directions are then bounced back from the cell's own slot.
 #pragma unroll
       for (int q = 0; q < 19; q++)
-        fi[j][q] = S::ldr(f + ((uint32_t)opp(q) * Np + p[j] - (uint32_t)a.off[q]));
+        fi[j][q] = toc<K>(S::ldr(f + ((uint32_t)opp(q) * Np + p[j] - (uint32_t)a.off[q])), q);
     } else {
 #pragma unroll
-      for (int q = 0; q < 19; q++) fi[j][q] = S::ldr(f + ((uint32_t)q * Np + p[j]));
+      for (int q = 0; q < 19; q++) fi[j][q] = toc<K>(S::ldr(f + ((uint32_t)q * Np + p[j])), q);
     }
     // running sums of the averages: loaded now, in flight with the populations
     if (ACC) {
@@ -107,19 +100,19 @@ __device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, cons
     if (ODD && m[j] != kMaskInterior) {
 #pragma unroll
       for (int q = 1; q < 19; q++)
-        if (!((m[j] >> q) & 1u)) fi[j][q] = S::ldr(f + ((uint32_t)q * Np + p[j]));
+        if (!((m[j] >> q) & 1u)) fi[j][q] = toc<K>(S::ldr(f + ((uint32_t)q * Np + p[j])), q);
     }
     const uint32_t cls = (m[j] >> kClassShift) & 3u;
     L nsv = (L)0;
     if (HAS_NS) nsv = (L)a.ns[p[j]];
     L fo[19], ux, uy, uz, rho;
     if constexpr (sizeof(L) == 4)
-      collide_fast<HAS_NS, S::kShifted>(fi[j], cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
+      collide_fast<HAS_NS, S::kCollideShifted, S::kFastMath>(fi[j], cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
     else collide<L, HAS_NS>(fi[j], cls, nsv, make_params<L>(a), fo, ux, uy, uz, rho);
     if (ODD && (sg[j].x & kSegInterior)) {
       // every neighbour is fluid: each population goes to the neighbour's slot (warp-uniform branch)
 #pragma unroll
-      for (int q = 0; q < 19; q++) S::str(f + ((uint32_t)q * Np + p[j] + (uint32_t)a.off[q]), fo[q]);
+      for (int q = 0; q < 19; q++) S::str(f + ((uint32_t)q * Np + p[j] + (uint32_t)a.off[q]), fromc<K>(fo[q], q));
     } else {
 #pragma unroll
       for (int q = 0; q < 19; q++) {
@@ -127,7 +120,7 @@ __device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, cons
         if (ODD)
           idx = ((m[j] >> opp(q)) & 1u) ? (uint32_t)q * Np + p[j] + (uint32_t)a.off[q] : (uint32_t)opp(q) * Np + p[j];
         else idx = (uint32_t)opp(q) * Np + p[j];
-        S::str(f + idx, fo[q]);
+        S::str(f + idx, fromc<K>(fo[q], q));
       }
     }
     if (ACC) {
@@ -138,6 +131,19 @@ __device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, cons
       acc[3u * Np + p[j]] = (Acc)((L)av[j][3] + rho);
     }
   }
+}
+
+// One warp's share of a step: SPW segments starting at s0 of the domain described by `a`.
+template <int K, bool ODD, bool ACC, bool HAS_NS, int SPW, class Args>
+__device__ __forceinline__ void step_warp(const Args &a, const uint32_t s0, const uint32_t lane) {
+  if (s0 >= a.nseg) return;
+  // the run-state word changes only between launches: a plain load issued together with the segment's
+  const int halted = a.status ? *a.status : 0;
+  uint2 sg[SPW];
+#pragma unroll
+  for (int j = 0; j < SPW; j++) sg[j] = (s0 + j < a.nseg) ? a.seg[s0 + j] : make_uint2(0, 0);
+  if (halted) return;
+  step_cells<K, ODD, ACC, HAS_NS, SPW>(a, sg, lane);
 }
 
 // Traversal order: blocks run in rising index order, so a step ends with the last segments' lines in

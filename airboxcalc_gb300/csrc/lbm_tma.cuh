@@ -265,27 +265,27 @@ __global__ void __launch_bounds__(kTmaThreads, 2)
       for (int q = 0; q < 19; q++) {
         if (ODD) {
           const T *row = (const T *)((const unsigned char *)sp + G::slot_off(q));
-          fi[q] = S::ldsr(row + (cz(q) == 0 ? lane : G::kPad + lane - cz(q)));
+          fi[q] = toc<K>(S::ldsr(row + (cz(q) == 0 ? lane : G::kPad + lane - cz(q))), q);
         } else {
-          fi[q] = S::ldsr(sp + q * 32 + lane);
+          fi[q] = toc<K>(S::ldsr(sp + q * 32 + lane), q);
         }
       }
       if (ODD && m != 0x7FFFFu) {
 #pragma unroll
         for (int q = 1; q < 19; q++)
-          if (!((m >> q) & 1u)) fi[q] = S::ldr(f + ((uint32_t)q * Np + p));  // bounce-back
+          if (!((m >> q) & 1u)) fi[q] = toc<K>(S::ldr(f + ((uint32_t)q * Np + p)), q);  // bounce-back
       }
       const uint32_t cls = (m >> kClassShift) & 3u;
       L nsv = (L)0;
       if (HAS_NS) nsv = (L)a.ns[p];
       L fo[19], ux, uy, uz, rho;
-      collide_fast<HAS_NS, S::kShifted>(fi, cls, nsv, CP, fo, ux, uy, uz, rho);
+      collide_fast<HAS_NS, S::kCollideShifted, S::kFastMath>(fi, cls, nsv, CP, fo, ux, uy, uz, rho);
 #pragma unroll
       for (int q = 0; q < 19; q++) {
         uint32_t idx;
         if (ODD) idx = ((m >> opp(q)) & 1u) ? (uint32_t)q * Np + p + (uint32_t)a.off[q] : (uint32_t)opp(q) * Np + p;
         else idx = (uint32_t)opp(q) * Np + p;
-        S::str(f + idx, fo[q]);
+        S::str(f + idx, fromc<K>(fo[q], q));
       }
       if (ACC) {
         const float *ac = (const float *)(base + ST::kAccOff + warp * 512);

@@ -399,6 +399,82 @@ cudaError_t prep_segments(const MaskArgs &a, int W, const uint32_t *bits, int64_
   return compact(it, (int64_t)a.nx * a.ny * S, seg, block_counts, offsets, st);
 }
 
+// ------------------------------------------------------------------ work lists of the vectorised step kernel
+// Item i of the block lists is block i % nb of segment i / nb (nb = 32 / V blocks per segment).  A block is
+// interior of class cls when its V cells are all fluid and every one's mask word is kMaskInterior with that
+// class in the class bits: all 18 pull neighbours fluid, no bounce-back, one collision branch.
+__device__ __forceinline__ bool vec_block_is(const uint2 s, const uint32_t *__restrict__ mask, int V, int blk,
+                                             uint32_t want) {
+  const uint32_t vm = (V >= 32) ? 0xffffffffu : ((1u << V) - 1u);
+  if (((s.y >> (blk * V)) & vm) != vm) return false;
+  const uint32_t base = seg_base(s) + (uint32_t)(blk * V);
+  for (int c = 0; c < V; c++)
+    if (mask[base + c] != want) return false;
+  return true;
+}
+constexpr uint32_t kMaskInteriorFilter = kMaskInterior | (kClsFilter << kClassShift);
+
+struct VecBlockItems {
+  const uint2 *seg;
+  const uint32_t *mask;
+  int V, nb;
+  uint32_t want;
+  __device__ bool hit(int64_t i) const { return vec_block_is(seg[i / nb], mask, V, (int)(i % nb), want); }
+  __device__ uint32_t value(int64_t i) const { return seg_base(seg[i / nb]) + (uint32_t)((i % nb) * V); }
+};
+struct VecBoundaryItems {   // segment i -> {base | interior flag, its fluid cells outside interior blocks}
+  const uint2 *seg;
+  const uint32_t *mask;
+  int V, nb;
+  __device__ uint32_t lanes(int64_t i) const {
+    const uint2 s = seg[i];
+    uint32_t out = s.y;
+    const uint32_t vm = (V >= 32) ? 0xffffffffu : ((1u << V) - 1u);
+    for (int b = 0; b < nb; b++)
+      if (vec_block_is(s, mask, V, b, kMaskInterior) || vec_block_is(s, mask, V, b, kMaskInteriorFilter))
+        out &= ~(vm << (b * V));
+    return out;
+  }
+  __device__ bool hit(int64_t i) const { return lanes(i) != 0u; }
+  __device__ uint2 value(int64_t i) const {
+    const uint2 s = seg[i];
+    const uint32_t l = lanes(i), base = seg_base(s);
+    bool interior = true;   // every remaining cell has all 18 neighbours fluid and the bulk class
+    for (int c = 0; c < 32; c++)
+      if (((l >> c) & 1u) && mask[base + c] != kMaskInterior) interior = false;
+    return make_uint2(base | (interior ? kSegInterior : 0u), l);
+  }
+};
+
+cudaError_t prep_vec_lists(const uint2 *seg, uint32_t nseg, const uint32_t *mask, int V, uint32_t *blk, uint2 *bseg,
+                           uint32_t *block_counts, unsigned long long *offsets, unsigned long long *counts,
+                           cudaStream_t st) {
+  if (V != 2 && V != 4 && V != 8) return cudaErrorInvalidValue;
+  const int nb = 32 / V;
+  const int64_t nitems = (int64_t)nseg * nb;
+  const int64_t nbb = prep_compact_blocks(nitems);
+  cudaError_t e;
+  // bulk blocks, then filter blocks behind them, then the boundary segments; counts[] receive the three totals
+  const VecBlockItems bulk{seg, mask, V, nb, kMaskInterior};
+  if ((e = compact(bulk, nitems, (uint32_t *)nullptr, block_counts, offsets, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(counts + 0, offsets + nbb, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  const VecBlockItems filt{seg, mask, V, nb, kMaskInteriorFilter};
+  if ((e = compact(filt, nitems, (uint32_t *)nullptr, block_counts, offsets, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(counts + 1, offsets + nbb, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  const VecBoundaryItems bnd{seg, mask, V, nb};
+  const int64_t nbs = prep_compact_blocks(nseg);
+  if ((e = compact(bnd, (int64_t)nseg, (uint2 *)nullptr, block_counts, offsets, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(counts + 2, offsets + nbs, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  if (!blk && !bseg) return cudaSuccess;
+  // the lists: the filter blocks are written behind the bulk blocks (their count is known on the host by now)
+  unsigned long long c[3];
+  if ((e = cudaMemcpyAsync(c, counts, sizeof c, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  if ((e = compact(bulk, nitems, blk, block_counts, offsets, st)) != cudaSuccess) return e;
+  if ((e = compact(filt, nitems, blk + c[0], block_counts, offsets, st)) != cudaSuccess) return e;
+  return compact(bnd, (int64_t)nseg, bseg, block_counts, offsets, st);
+}
+
 // ------------------------------------------------------------------ opening search (src/engine.js:141-171)
 constexpr uint32_t kClaimFree = 0xFFFFFFFFu, kClaimDone = 0xFFFFFFFEu;
 

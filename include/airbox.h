@@ -25,7 +25,7 @@ extern "C" {
 
 /* Version of the structures and entry points below; a host compares it with abx_abi_version() before use.
  * 2: prepare timings in abx_geom_info, coordinate channels in abx_net_params, batch groups.
- * 3: abx_run_params.flags (bfloat16 storage only on request). */
+ * 3: abx_run_params.flags (bfloat16 storage only on request), vectorised-kernel fields in abx_sim_info. */
 #define ABX_ABI_VERSION 3
 
 /* Status codes.  The first group mirrors the errors engine.js throws. */
@@ -146,6 +146,9 @@ typedef struct {
   int64_t Np;                   /* padded cells held on the device */
   int64_t state_bytes;          /* device bytes of populations + averages */
   int tma_pipeline;             /* 1 when the step kernel is fed by TMA tensor copies */
+  int vec_width;                /* cells per thread of the vectorised step kernel (0: one cell per lane) */
+  int64_t vec_interior_cells;   /* fluid cells it moves as vectors (known after the first step; the rest
+                                   run one per lane) */
 } abx_sim_info;
 int abx_sim_get_info(const abx_sim *s, abx_sim_info *out);
 
