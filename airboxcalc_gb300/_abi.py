@@ -112,9 +112,12 @@ class TrainParams(C.Structure):
                 ("lr", C.c_double), ("lr_min", C.c_double), ("seed", C.c_ulonglong), ("flip", C.c_int)]
 
 
+RULE_CHANGE, RULE_STDERR = 0, 1  # include/airbox.h ABX_RULE_*
+
+
 class ConvergeParams(C.Structure):
     _fields_ = [("settle", C.c_int), ("window", C.c_int), ("min_avg", C.c_int), ("max_steps", C.c_int),
-                ("tol", C.c_double)]
+                ("tol", C.c_double), ("rule", C.c_int), ("min_windows", C.c_int)]
 
 
 class ConvergeResult(C.Structure):

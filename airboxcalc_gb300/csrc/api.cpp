@@ -161,14 +161,14 @@ struct abx_geom {
   struct VecLists {
     bool ready = false;
     uint32_t *d_blk = nullptr;
-    uint2 *d_bseg = nullptr;
-    uint32_t n_bulk = 0, n_filter = 0, nbseg = 0;
+    uint32_t *d_bcell = nullptr;
+    uint32_t n_bulk = 0, n_filter = 0, nbcell = 0;
   } vec[3];
   ~abx_geom() {
     cudaSetDevice(device);
     cudaFree(d_solid); cudaFree(d_fluid); cudaFree(d_outlet);
     cudaFree(d_mask); cudaFree(d_seg); cudaFree(d_opening); cudaFree(d_cells);
-    for (auto &v : vec) { cudaFree(v.d_blk); cudaFree(v.d_bseg); }
+    for (auto &v : vec) { cudaFree(v.d_blk); cudaFree(v.d_bcell); }
   }
 };
 
@@ -680,6 +680,7 @@ struct abx_sim {
   int *d_status = nullptr;
   unsigned long long *d_diag = nullptr;
   double *d_hist = nullptr, *d_eval = nullptr;
+  void *d_acc_snap = nullptr;      // running sums at the start of the convergence run's current window
   float *d_fmap = nullptr;
   int64_t *d_plist = nullptr;
   float *d_probe_vy = nullptr;     // probe scratch: -u_y of every probe cell
@@ -709,7 +710,7 @@ struct abx_sim {
     free_tma(&tma);
     for (auto e : ev_pool) cudaEventDestroy(e);
     cudaFree(d_f); cudaFree(d_acc); cudaFree(d_ns); cudaFree(d_status); cudaFree(d_diag); cudaFree(d_hist);
-    cudaFree(d_eval);
+    cudaFree(d_eval); cudaFree(d_acc_snap);
     cudaFree(d_fmap); cudaFree(d_plist); cudaFree(d_probe_vy); cudaFree(d_probe_part);
     if (st) cudaStreamDestroy(st);
   }
@@ -763,7 +764,7 @@ static int geom_vec_lists(abx_geom &g, int V, cudaStream_t st) {
   abx_geom::VecLists &L = g.vec[vi];
   if (L.ready) return ABX_OK;
   CK(cudaSetDevice(g.device), "vector lists: set device");
-  const int64_t items = (int64_t)g.nseg * (32 / V);
+  const int64_t items = (int64_t)g.nseg * 32;
   const int64_t nb = prep_compact_blocks(std::max<int64_t>(items, 1));
   DevBuf dbc, doff, dcnt;
   CK(cudaMalloc(&dbc.p, sizeof(uint32_t) * std::max<int64_t>(nb, 1)), "vector lists");
@@ -775,19 +776,20 @@ static int geom_vec_lists(abx_geom &g, int V, cudaStream_t st) {
   CK(cudaMemcpyAsync(c, dcnt.p, sizeof c, cudaMemcpyDeviceToHost, st), "vector lists");
   CK(cudaStreamSynchronize(st), "vector lists");
   CK(cudaMalloc((void **)&L.d_blk, sizeof(uint32_t) * std::max<unsigned long long>(c[0] + c[1], 1)), "vector lists");
-  CK(cudaMalloc((void **)&L.d_bseg, sizeof(uint2) * std::max<unsigned long long>(c[2], 1)), "vector lists");
-  CK(prep_vec_lists(g.d_seg, g.nseg, g.d_mask, V, L.d_blk, L.d_bseg, (uint32_t *)dbc.p, (unsigned long long *)doff.p,
+  CK(cudaMalloc((void **)&L.d_bcell, sizeof(uint32_t) * std::max<unsigned long long>(c[2], 1)), "vector lists");
+  CK(prep_vec_lists(g.d_seg, g.nseg, g.d_mask, V, L.d_blk, L.d_bcell, (uint32_t *)dbc.p, (unsigned long long *)doff.p,
                     (unsigned long long *)dcnt.p, st), "vector lists: write");
   CK(cudaStreamSynchronize(st), "vector lists");
-  L.n_bulk = (uint32_t)c[0]; L.n_filter = (uint32_t)c[1]; L.nbseg = (uint32_t)c[2];
+  L.n_bulk = (uint32_t)c[0]; L.n_filter = (uint32_t)c[1]; L.nbcell = (uint32_t)c[2];
   L.ready = true;
   return ABX_OK;
 }
 
-// Block width of the vectorised step kernel for a storage (ABX_VEC=0: the one-cell-per-lane kernel everywhere;
-// ABX_VEC_V=n: that width where the storage has it).
+// Block width of the vectorised step kernel for a storage; opt-in with ABX_VEC=1 (ABX_VEC_V=n: that width where the
+// storage has it).  The one-cell-per-lane kernel is the default: it is the faster of the two on GB300.
 static int vec_width(int storage) {
-  if (const char *e = std::getenv("ABX_VEC")) if (e[0] == '0') return 0;
+  const char *on = std::getenv("ABX_VEC");
+  if (!on || on[0] != '1') return 0;
   int want = 0;
   if (const char *e = std::getenv("ABX_VEC_V")) want = std::atoi(e);
   switch (storage) {
@@ -865,6 +867,7 @@ extern "C" int abx_sim_create(abx_geom *g, const abx_run_params *p, const float 
   // the vectorised step kernel (not with a partial bounce-back field, nor next to the opt-in TMA kernel); its
   // work lists are built before the first step
   if (!ns && !s.tma.ready) s.vec_V = vec_width(p->storage);
+  if (s.vec_V) CK(prepare_step_vec(p->storage, s.vec_V), "sim_create: vector kernel");
   int rc = sim_reset(&s);
   if (rc) return rc;
   s.h2d = create_h2d;
@@ -911,7 +914,7 @@ static int run_steps(abx_sim *s, int n, bool acc) {
     if (int rc = geom_vec_lists(*s->g, s->vec_V, s->st)) return rc;
     const abx_geom::VecLists &L = s->g->vec[vec_index(s->vec_V)];
     s->va.blk = L.d_blk; s->va.n_bulk = L.n_bulk; s->va.n_filter = L.n_filter;
-    s->va.bseg = L.d_bseg; s->va.nbseg = L.nbseg;
+    s->va.bcell = L.d_bcell; s->va.nbcell = L.nbcell;
     s->va_ready = true;
   }
   if (!s->use_graphs) {
@@ -1136,9 +1139,18 @@ extern "C" int abx_sim_get_acc(abx_sim *s, float *acc) {
   return ABX_OK;
 }
 
+static int sim_evaluate(abx_sim *s, abx_metrics *m, float *fmap, double *hist, int hist_cap, int *nhist,
+                        const void *base, int base_nacc);
+
 extern "C" int abx_sim_evaluate(abx_sim *s, abx_metrics *m, float *fmap, double *hist, int hist_cap, int *nhist) {
   clear_stale_error();
   if (!s || !m) return fail(ABX_ERR_INVALID_ARGUMENT, "sim_evaluate: null argument");
+  return sim_evaluate(s, m, fmap, hist, hist_cap, nhist, nullptr, 0);
+}
+
+// evaluate() of the running averages, or (base != null) of the averages of the steps since the snapshot base
+static int sim_evaluate(abx_sim *s, abx_metrics *m, float *fmap, double *hist, int hist_cap, int *nhist,
+                        const void *base, int base_nacc) {
   CK(cudaSetDevice(s->g->device), "sim_evaluate");
   const abx_geom &g = *s->g;
   EvalArgs e{};
@@ -1146,6 +1158,7 @@ extern "C" int abx_sim_evaluate(abx_sim *s, abx_metrics *m, float *fmap, double 
   e.jb = first_ge(g.dc, g.pleat + 2 * g.h);
   e.nacc = s->nacc; e.u0 = s->u0; e.opening = g.d_opening; e.ns = s->has_ns ? s->d_ns : nullptr;
   e.fmap = s->d_fmap; e.out = s->d_eval;
+  e.base = base; e.base_nacc = base_nacc;
   cudaEvent_t v0 = nullptr, v1 = nullptr;
   if (s->timing) { v0 = next_event(s); v1 = next_event(s); if (v0 && v1) { cudaEventRecord(v0, s->st); s->ev_kind.push_back(3); s->ev_nsteps.push_back(0); } }
   CK(launch_evaluate(s->p.storage, state_args(*s), e, s->st), "sim_evaluate");
@@ -1401,33 +1414,67 @@ extern "C" int abx_sim_converge(abx_sim *s, const abx_converge_params *p, abx_co
   if (p->settle < 0 || p->window <= 0 || p->min_avg < p->window || p->max_steps < p->settle + p->window || !(p->tol > 0))
     return fail(ABX_ERR_INVALID_ARGUMENT,
                 "sim_converge: settle >= 0, window > 0, min_avg >= window, max_steps >= settle + window and tol > 0 required");
+  if (p->rule != ABX_RULE_CHANGE && p->rule != ABX_RULE_STDERR)
+    return fail(ABX_ERR_INVALID_ARGUMENT, "sim_converge: unknown stop rule %d", p->rule);
+  if (p->rule == ABX_RULE_STDERR && p->min_windows < 2)
+    return fail(ABX_ERR_INVALID_ARGUMENT, "sim_converge: the standard-error rule needs min_windows >= 2");
   CK(cudaSetDevice(s->g->device), "sim_converge");
   std::memset(r, 0, sizeof *r);
   r->change = INFINITY;
+  const size_t acc_sz = acc_bytes(s->p.storage) * 4 * (size_t)s->g->Np;
+  if (p->rule == ABX_RULE_STDERR && !s->d_acc_snap) CK(cudaMalloc(&s->d_acc_snap, acc_sz), "sim_converge: snapshot");
   if (p->settle > 0) {
     if (int rc = run_steps(s, p->settle, false)) return rc;
     r->steps = p->settle;
   }
-  CK(cudaMemsetAsync(s->d_acc, 0, acc_bytes(s->p.storage) * 4 * (size_t)s->g->Np, s->st), "sim_converge");
+  CK(cudaMemsetAsync(s->d_acc, 0, acc_sz, s->st), "sim_converge");
   s->nacc = 0;
   double pg = NAN, pz = NAN;
+  std::vector<double> wg, wz;   // the windows' own gamma core and zeta (standard-error rule)
   while (r->steps + p->window <= p->max_steps) {
+    const int snap_nacc = s->nacc;
+    if (p->rule == ABX_RULE_STDERR)
+      CK(cudaMemcpyAsync(s->d_acc_snap, s->d_acc, acc_sz, cudaMemcpyDeviceToDevice, s->st), "sim_converge: snapshot");
     if (int rc = run_steps(s, p->window, true)) return rc;
     abx_metrics m;
-    if (int rc = abx_sim_evaluate(s, &m, nullptr, nullptr, 0, nullptr)) return rc;
+    if (int rc = sim_evaluate(s, &m, nullptr, nullptr, 0, nullptr, nullptr, 0)) return rc;
     r->steps += p->window;
     r->windows++;
     r->metrics = m;
     if (!std::isfinite(m.gammaCore) || !std::isfinite(m.zeta))
       return fail(ABX_ERR_UNSTABLE, "Rechnung instabil bei Schritt %d. Zellgröße vergrößern oder Viskosität (tau) erhöhen.", s->step);
-    if (r->windows >= 2)
-      r->change = std::max(std::fabs(m.gammaCore - pg) / std::fabs(m.gammaCore), std::fabs(m.zeta - pz) / std::fabs(m.zeta));
-    if (s->nacc >= p->min_avg && r->change < p->tol) {
-      r->converged = 1;
-      break;
+    if (p->rule == ABX_RULE_CHANGE) {
+      if (r->windows >= 2)
+        r->change = std::max(std::fabs(m.gammaCore - pg) / std::fabs(m.gammaCore), std::fabs(m.zeta - pz) / std::fabs(m.zeta));
+      if (s->nacc >= p->min_avg && r->change < p->tol) {
+        r->converged = 1;
+        break;
+      }
+      pg = m.gammaCore;
+      pz = m.zeta;
+    } else {
+      abx_metrics mw;
+      if (int rc = sim_evaluate(s, &mw, nullptr, nullptr, 0, nullptr, s->d_acc_snap, snap_nacc)) return rc;
+      wg.push_back(mw.gammaCore);
+      wz.push_back(mw.zeta);
+      const size_t n = wg.size();
+      if (n >= 2) {
+        // batch means: standard error of the mean of the n window averages, relative to the running average
+        auto rel_se = [n](const std::vector<double> &v, double ref) {
+          double mean = 0;
+          for (double x : v) mean += x;
+          mean /= (double)n;
+          double ss = 0;
+          for (double x : v) ss += (x - mean) * (x - mean);
+          return std::sqrt(ss / (double)(n - 1) / (double)n) / std::fabs(ref);
+        };
+        r->change = std::max(rel_se(wg, m.gammaCore), rel_se(wz, m.zeta));
+      }
+      if ((int)n >= p->min_windows && s->nacc >= p->min_avg && r->change <= 0.5 * p->tol) {
+        r->converged = 1;
+        break;
+      }
     }
-    pg = m.gammaCore;
-    pz = m.zeta;
   }
   return ABX_OK;
 }

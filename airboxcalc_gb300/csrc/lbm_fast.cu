@@ -60,9 +60,47 @@ static cudaError_t step_k(bool odd, bool acc, bool has_ns, const StepArgs &a, cu
 }
 
 // ------------------------------------------------------------------ vectorised step (V cells per thread)
+template <class... KArgs, class... Args>
+static cudaError_t launch_vec_kernel(void (*kern)(KArgs...), unsigned grid, unsigned threads, size_t smem,
+                                     cudaStream_t st, Args &&...args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = ABX_PDL ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
+template <int K, int V>
+static cudaError_t vec_attrs() {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(aa_vec_kernel<K, V, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                vec_smem_bytes<K, V, true>())) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(aa_vec_kernel<K, V, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                vec_smem_bytes<K, V, true>())) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(aa_vec_kernel<K, V, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                vec_smem_bytes<K, V, false>())) != cudaSuccess) return e;
+  return cudaFuncSetAttribute(aa_vec_kernel<K, V, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              vec_smem_bytes<K, V, false>());
+}
+
+cudaError_t prepare_step_vec(int storage, int V) {
+  switch (storage) {
+    case kStoreF32: if (V == 4) return vec_attrs<kStoreF32, 4>(); if (V == 2) return vec_attrs<kStoreF32, 2>(); break;
+    case kStoreF16: if (V == 4) return vec_attrs<kStoreF16, 4>(); if (V == 2) return vec_attrs<kStoreF16, 2>(); break;
+    case kStoreBF16: if (V == 4) return vec_attrs<kStoreBF16, 4>(); if (V == 2) return vec_attrs<kStoreBF16, 2>(); break;
+  }
+  return cudaErrorInvalidValue;
+}
+
 template <int K, int V>
 static cudaError_t step_vec_k(bool odd, bool acc, const StepArgs &a, const VecArgs &v, cudaStream_t st) {
-  const uint32_t items = (v.n_bulk + 31u) / 32u + (v.n_filter + 31u) / 32u + v.nbseg;
+  const uint32_t items = (v.n_bulk + 31u) / 32u + (v.n_filter + 31u) / 32u + (v.nbcell + 31u) / 32u;
   if (items == 0) return cudaSuccess;
   static int nsm = 0;
   if (!nsm) {
@@ -75,11 +113,11 @@ static cudaError_t step_vec_k(bool odd, bool acc, const StepArgs &a, const VecAr
   const unsigned need = (items + W - 1) / W, res = (unsigned)nsm * VecShape<K, V>::kMinBlocks;
   const unsigned grid = need < res ? need : res;
   if (odd) {
-    if (acc) return launch_step_kernel_t(aa_vec_kernel<K, V, true, true>, grid, T, st, a, v);
-    return launch_step_kernel_t(aa_vec_kernel<K, V, true, false>, grid, T, st, a, v);
+    if (acc) return launch_vec_kernel(aa_vec_kernel<K, V, true, true>, grid, T, vec_smem_bytes<K, V, true>(), st, a, v);
+    return launch_vec_kernel(aa_vec_kernel<K, V, true, false>, grid, T, vec_smem_bytes<K, V, false>(), st, a, v);
   }
-  if (acc) return launch_step_kernel_t(aa_vec_kernel<K, V, false, true>, grid, T, st, a, v);
-  return launch_step_kernel_t(aa_vec_kernel<K, V, false, false>, grid, T, st, a, v);
+  if (acc) return launch_vec_kernel(aa_vec_kernel<K, V, false, true>, grid, T, vec_smem_bytes<K, V, true>(), st, a, v);
+  return launch_vec_kernel(aa_vec_kernel<K, V, false, false>, grid, T, vec_smem_bytes<K, V, false>(), st, a, v);
 }
 
 cudaError_t launch_step_vec(int storage, int V, bool odd, bool acc, const StepArgs &a, const VecArgs &v,

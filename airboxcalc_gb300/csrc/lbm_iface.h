@@ -60,6 +60,8 @@ struct EvalArgs {
   const float *ns;         // padded, or null
   float *fmap;             // nx*nz, or null
   double *out;             // 13 doubles
+  const void *base;        // null, or running sums to subtract (same type as acc): the averages of the steps since
+  int base_nacc;           // that snapshot, which held base_nacc steps
 };
 
 // TMA descriptors of one simulation: five CUtensorMap (made by make_tma,
@@ -77,21 +79,23 @@ void free_tma(TmaBlob *b);
 
 // Work lists of the vectorised step kernel (lbm_vec.cuh), built per geometry and block width V (cells per
 // thread, consecutive along k): interior blocks - V fluid cells whose 18 pull neighbours are all fluid, all of
-// class bulk or all of class filter - and the remaining fluid cells as boundary segments.
+// class bulk or all of class filter - and every other fluid cell in a dense list (one per lane).
 struct VecArgs {
   const uint32_t *blk;     // padded index of the first cell of every interior block: bulk blocks, then filter blocks
   uint32_t n_bulk, n_filter;
-  const uint2 *bseg;       // boundary segments {base | kSegInterior flag, lane mask of their cells}
-  uint32_t nbseg;
+  const uint32_t *bcell;   // padded index of every fluid cell outside the interior blocks, rising
+  uint32_t nbcell;
 };
-// The lists of a geometry for block width V (4 or 8): call with blk == bseg == nullptr to get the three
-// counts (counts[0..2] = bulk blocks, filter blocks, boundary segments), then with arrays of those sizes.
-// block_counts / offsets: scratch of prep_compact_blocks(nseg * 32 / V) and + 1 entries.
-cudaError_t prep_vec_lists(const uint2 *seg, uint32_t nseg, const uint32_t *mask, int V, uint32_t *blk, uint2 *bseg,
-                           uint32_t *block_counts, unsigned long long *offsets, unsigned long long *counts,
-                           cudaStream_t st);
-// One step through the vectorised kernel (lbm_fast.cu; float32 with V = 4, float16 / bfloat16 with V = 4 or 8;
-// no partial bounce-back field).
+// The lists of a geometry for block width V (2, 4 or 8): call with blk == bcell == nullptr to get the three
+// counts (counts[0..2] = bulk blocks, filter blocks, boundary cells), then with arrays of those sizes.
+// block_counts / offsets: scratch of prep_compact_blocks(nseg * 32) and + 1 entries.
+cudaError_t prep_vec_lists(const uint2 *seg, uint32_t nseg, const uint32_t *mask, int V, uint32_t *blk,
+                           uint32_t *bcell, uint32_t *block_counts, unsigned long long *offsets,
+                           unsigned long long *counts, cudaStream_t st);
+// Shared-memory limits of the vectorised kernels for a storage and V (call once, outside stream capture).
+cudaError_t prepare_step_vec(int storage, int V);
+// One step through the vectorised kernel (lbm_fast.cu; float32, float16 and bfloat16 with V = 2 or 4; no partial
+// bounce-back field).
 cudaError_t launch_step_vec(int storage, int V, bool odd, bool acc, const StepArgs &a, const VecArgs &v,
                             cudaStream_t st);
 

@@ -397,7 +397,9 @@ __global__ void __launch_bounds__(1024) evaluate_kernel(const StateArgs a, EvalA
   const Acc *acc = (const Acc *)a.acc;
   const int nx = e.nx, ny = e.ny, nz = e.nz;
   const int64_t nzp = e.nzp, kpad = e.kpad;
-  const double dn = e.nacc > 1 ? (double)e.nacc : 1.0;
+  const Acc *base = (const Acc *)e.base;
+  const int nacc = base ? e.nacc - e.base_nacc : e.nacc;
+  const double dn = nacc > 1 ? (double)nacc : 1.0;
   auto P = [&](int i, int j, int k) -> int64_t { return ((int64_t)i * ny + j) * nzp + k + kpad; };
   auto fluid = [&](int64_t p) -> bool {
     if (!(a.mask[p] & kFluidBit)) return false;
@@ -405,7 +407,8 @@ __global__ void __launch_bounds__(1024) evaluate_kernel(const StateArgs a, EvalA
   };
   // mean field as the reference holds it: float32(acc / nacc); the float64 run keeps float64
   auto mean = [&](int c, int64_t p) -> double {
-    const double m = (double)acc[(int64_t)c * a.Np + p] / dn;
+    const int64_t i = (int64_t)c * a.Np + p;
+    const double m = (base ? (double)acc[i] - (double)base[i] : (double)acc[i]) / dn;
     if constexpr (sizeof(Acc) == 8) return m;
     else return (double)(float)m;
   };

@@ -422,57 +422,47 @@ struct VecBlockItems {
   __device__ bool hit(int64_t i) const { return vec_block_is(seg[i / nb], mask, V, (int)(i % nb), want); }
   __device__ uint32_t value(int64_t i) const { return seg_base(seg[i / nb]) + (uint32_t)((i % nb) * V); }
 };
-struct VecBoundaryItems {   // segment i -> {base | interior flag, its fluid cells outside interior blocks}
+struct VecBoundaryCells {   // cell i % 32 of segment i / 32 -> its padded index, if fluid and not in an interior block
   const uint2 *seg;
   const uint32_t *mask;
-  int V, nb;
-  __device__ uint32_t lanes(int64_t i) const {
-    const uint2 s = seg[i];
-    uint32_t out = s.y;
-    const uint32_t vm = (V >= 32) ? 0xffffffffu : ((1u << V) - 1u);
-    for (int b = 0; b < nb; b++)
-      if (vec_block_is(s, mask, V, b, kMaskInterior) || vec_block_is(s, mask, V, b, kMaskInteriorFilter))
-        out &= ~(vm << (b * V));
-    return out;
+  int V;
+  __device__ bool hit(int64_t i) const {
+    const uint2 s = seg[i / 32];
+    const int lane = (int)(i % 32), b = lane / V;
+    if (!((s.y >> lane) & 1u)) return false;
+    return !vec_block_is(s, mask, V, b, kMaskInterior) && !vec_block_is(s, mask, V, b, kMaskInteriorFilter);
   }
-  __device__ bool hit(int64_t i) const { return lanes(i) != 0u; }
-  __device__ uint2 value(int64_t i) const {
-    const uint2 s = seg[i];
-    const uint32_t l = lanes(i), base = seg_base(s);
-    bool interior = true;   // every remaining cell has all 18 neighbours fluid and the bulk class
-    for (int c = 0; c < 32; c++)
-      if (((l >> c) & 1u) && mask[base + c] != kMaskInterior) interior = false;
-    return make_uint2(base | (interior ? kSegInterior : 0u), l);
-  }
+  __device__ uint32_t value(int64_t i) const { return seg_base(seg[i / 32]) + (uint32_t)(i % 32); }
 };
 
-cudaError_t prep_vec_lists(const uint2 *seg, uint32_t nseg, const uint32_t *mask, int V, uint32_t *blk, uint2 *bseg,
-                           uint32_t *block_counts, unsigned long long *offsets, unsigned long long *counts,
-                           cudaStream_t st) {
+cudaError_t prep_vec_lists(const uint2 *seg, uint32_t nseg, const uint32_t *mask, int V, uint32_t *blk,
+                           uint32_t *bcell, uint32_t *block_counts, unsigned long long *offsets,
+                           unsigned long long *counts, cudaStream_t st) {
   if (V != 2 && V != 4 && V != 8) return cudaErrorInvalidValue;
   const int nb = 32 / V;
-  const int64_t nitems = (int64_t)nseg * nb;
-  const int64_t nbb = prep_compact_blocks(nitems);
+  const int64_t nitems = (int64_t)nseg * nb, ncells = (int64_t)nseg * 32;
   cudaError_t e;
-  // bulk blocks, then filter blocks behind them, then the boundary segments; counts[] receive the three totals
+  // bulk blocks, then filter blocks behind them, then the boundary cells; counts[] receive the three totals
   const VecBlockItems bulk{seg, mask, V, nb, kMaskInterior};
   if ((e = compact(bulk, nitems, (uint32_t *)nullptr, block_counts, offsets, st)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyAsync(counts + 0, offsets + nbb, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(counts + 0, offsets + prep_compact_blocks(nitems), sizeof(unsigned long long),
+                           cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
   const VecBlockItems filt{seg, mask, V, nb, kMaskInteriorFilter};
   if ((e = compact(filt, nitems, (uint32_t *)nullptr, block_counts, offsets, st)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyAsync(counts + 1, offsets + nbb, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
-  const VecBoundaryItems bnd{seg, mask, V, nb};
-  const int64_t nbs = prep_compact_blocks(nseg);
-  if ((e = compact(bnd, (int64_t)nseg, (uint2 *)nullptr, block_counts, offsets, st)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyAsync(counts + 2, offsets + nbs, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
-  if (!blk && !bseg) return cudaSuccess;
+  if ((e = cudaMemcpyAsync(counts + 1, offsets + prep_compact_blocks(nitems), sizeof(unsigned long long),
+                           cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  const VecBoundaryCells bnd{seg, mask, V};
+  if ((e = compact(bnd, ncells, (uint32_t *)nullptr, block_counts, offsets, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(counts + 2, offsets + prep_compact_blocks(ncells), sizeof(unsigned long long),
+                           cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  if (!blk && !bcell) return cudaSuccess;
   // the lists: the filter blocks are written behind the bulk blocks (their count is known on the host by now)
   unsigned long long c[3];
   if ((e = cudaMemcpyAsync(c, counts, sizeof c, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
   if ((e = compact(bulk, nitems, blk, block_counts, offsets, st)) != cudaSuccess) return e;
   if ((e = compact(filt, nitems, blk + c[0], block_counts, offsets, st)) != cudaSuccess) return e;
-  return compact(bnd, (int64_t)nseg, bseg, block_counts, offsets, st);
+  return compact(bnd, ncells, bcell, block_counts, offsets, st);
 }
 
 // ------------------------------------------------------------------ opening search (src/engine.js:141-171)

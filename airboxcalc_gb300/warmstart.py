@@ -36,7 +36,7 @@ WEIGHTS = os.path.join(HERE, "weights", "warmstart_r64_b16_l4.npz")
 RUN = dict(K=3, aniso=10, u=0.06, tau=0.51, steps=6000, avg=2000, every=150)
 K_CHOICES = (1.5, 3.0, 6.0)
 # Stop rule of the convergence run: settle, then a running average checked every window.
-CONVERGE = dict(settle=1000, window=500, min_avg=1000, max_steps=4000, tol=0.01)
+CONVERGE = dict(settle=1000, window=500, min_avg=1000, max_steps=4000, tol=0.01, rule=0, min_windows=4)
 
 
 def variant(seed: int, dx: float = 2.0):
@@ -152,7 +152,8 @@ def _metrics(m: A.Metrics) -> dict:
 def _converge_params(**kw) -> A.ConvergeParams:
     c = dict(CONVERGE, **kw)
     return A.ConvergeParams(settle=int(c["settle"]), window=int(c["window"]), min_avg=int(c["min_avg"]),
-                            max_steps=int(c["max_steps"]), tol=float(c["tol"]))
+                            max_steps=int(c["max_steps"]), tol=float(c["tol"]), rule=int(c["rule"]),
+                            min_windows=int(c["min_windows"]))
 
 
 def warm_start(sim: E.Simulation, net: Net):

@@ -358,24 +358,34 @@ int abx_net_predict(abx_net *n, abx_sim *s, float *features, float *pred);
  * averages and step count cleared. */
 int abx_sim_warm_start(abx_sim *s, abx_net *n);
 
+/* Stop rules of the convergence run. */
+#define ABX_RULE_CHANGE 0   /* the running average's gamma core and zeta moved less than tol over the last window */
+#define ABX_RULE_STDERR 1   /* batch means: the standard error of gamma core and zeta, estimated from the
+                               scatter of the windows' own averages (at least min_windows of them), is at most
+                               tol / 2 of the running average's value */
+
 typedef struct {
   int settle;               /* steps before averaging starts */
   int window;               /* steps between checks of the running average */
   int min_avg;              /* averaged steps before the stop rule may fire */
   int max_steps;            /* give up after this many steps (settle included) */
-  double tol;               /* stop when gamma core and zeta of the running average moved less than tol
-                               (relative) over the last window */
+  double tol;               /* relative tolerance of the stop rule */
+  int rule;                 /* ABX_RULE_CHANGE or ABX_RULE_STDERR */
+  int min_windows;          /* ABX_RULE_STDERR: windows before the standard error counts (>= 2) */
 } abx_converge_params;
 
 typedef struct {
   abx_metrics metrics;      /* evaluate() of the running average at the stop */
   int steps, windows, converged;
-  double change;            /* last window's relative change of the running average's KPIs */
+  double change;            /* ABX_RULE_CHANGE: last window's relative change of the running average's KPIs;
+                               ABX_RULE_STDERR: the larger relative standard error of gamma core and zeta */
 } abx_converge_result;
 
 /* Convergence run from the current state: `settle` steps, then steps added to
  * a running average, evaluated every `window` steps, until the stop rule
- * fires or max_steps.  Non-finite KPIs end the run with ABX_ERR_UNSTABLE. */
+ * (`rule`, see ABX_RULE_*) fires or max_steps.  Non-finite KPIs end the run
+ * with ABX_ERR_UNSTABLE.  The standard-error rule keeps a copy of the running
+ * sums (4 values per padded cell) on the device from its first call on. */
 int abx_sim_converge(abx_sim *s, const abx_converge_params *p, abx_converge_result *r);
 
 typedef struct {

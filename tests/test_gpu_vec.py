@@ -41,6 +41,7 @@ def run(g, storage, steps_plain, steps_acc):
 @pytest.mark.parametrize("storage,V", [("f32", 2), ("f32", 4), ("f16", 2), ("f16", 4), ("bf16", 4)])
 def test_vec_kernel_matches_one_cell_kernel(name, storage, V, monkeypatch):
     g = geom(name)
+    monkeypatch.setenv("ABX_VEC", "1")
     monkeypatch.setenv("ABX_VEC_V", str(V))
     f, acc, info = run(g, storage, 7, 6)
     assert info.vec_width == V
