@@ -158,6 +158,37 @@ def test_converge_and_fallback_to_the_reference_schedule():
     assert res["total_ms"] >= res["infer_ms"] > 0
 
 
+def test_standard_error_stop_rule():
+    """ABX_RULE_STDERR: the windows' own KPIs (evaluated from the running sums minus a snapshot taken at the
+    window's start) give the batch-means standard error the rule compares with tol / 2.  A twin simulation that
+    restarts its averages at every window reproduces the windows' KPIs, and from them the same standard error."""
+    g = geometry()
+    net = W.Net(16, 8, 2, seed=5)
+    rule = dict(settle=20, window=20, min_avg=40, max_steps=140, tol=1e-12, rule=1, min_windows=3)
+    S = E.Simulation(g, RUN)
+    W.warm_start(S, net)
+    r = W.converge(S, **rule)
+    assert not r["converged"] and r["steps"] == 140 and r["windows"] == 6
+    T = E.Simulation(g, RUN)
+    W.warm_start(T, net)
+    T.step(20)
+    wg, wz = [], []
+    for _ in range(6):
+        T.clear_acc()
+        T.step(20, True)
+        m = T.evaluate()["metrics"]
+        wg.append(m["gammaCore"])
+        wz.append(m["zeta"])
+    run_g, run_z = r["metrics"]["gammaCore"], r["metrics"]["zeta"]
+    se = max(np.std(wg, ddof=1) / np.sqrt(6) / abs(run_g), np.std(wz, ddof=1) / np.sqrt(6) / abs(run_z))
+    assert r["change"] == pytest.approx(se, rel=1e-3)
+    # a loose tolerance fires once min_windows windows and min_avg steps are in
+    S2 = E.Simulation(g, RUN)
+    W.warm_start(S2, net)
+    r2 = W.converge(S2, **dict(rule, tol=10.0))
+    assert r2["converged"] and r2["windows"] == 3 and r2["change"] <= 5.0
+
+
 def test_net_argument_errors():
     with pytest.raises(E.AirboxError):
         W.Net(12, 8, 2)            # not a power of two
