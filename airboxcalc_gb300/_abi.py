@@ -30,7 +30,7 @@ EXPORTS = [
     "abx_sim_get_info", "abx_sim_reset", "abx_sim_step", "abx_sim_run", "abx_sim_get_f", "abx_sim_set_f",
     "abx_sim_get_acc", "abx_sim_clear_acc", "abx_sim_evaluate", "abx_simulate", "abx_sim_set_timing", "abx_sim_get_timing",
     "abx_voxelize_static",
-    "abx_net_create", "abx_net_free", "abx_net_get_info", "abx_net_get_weights", "abx_net_set_weights",
+    "abx_net_create", "abx_net_set_tensor_cores", "abx_net_free", "abx_net_get_info", "abx_net_get_weights", "abx_net_set_weights",
     "abx_net_add_sample", "abx_net_clear_samples", "abx_net_get_sample", "abx_net_train", "abx_net_eval_loss",
     "abx_net_forward_backward", "abx_net_predict", "abx_sim_warm_start", "abx_sim_converge", "abx_sim_solve_warm",
     "abx_batch_create", "abx_batch_free", "abx_batch_sim", "abx_batch_tune", "abx_batch_set_shape", "abx_batch_reset",
@@ -104,7 +104,8 @@ class NetParams(C.Structure):
 
 class NetInfo(C.Structure):
     _fields_ = [("res", C.c_int), ("base", C.c_int), ("levels", C.c_int), ("in_channels", C.c_int),
-                ("out_channels", C.c_int), ("n_samples", C.c_int), ("n_params", C.c_longlong)]
+                ("out_channels", C.c_int), ("n_samples", C.c_int), ("n_params", C.c_longlong),
+                ("tensor_cores", C.c_int)]
 
 
 class TrainParams(C.Structure):

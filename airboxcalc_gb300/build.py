@@ -6,6 +6,7 @@ Translation units, compiled in parallel:
   csrc/lbm_fast.cu   nvcc (float32 / float16 / bfloat16 step kernels, FMA contraction allowed)
   csrc/warmstart.cu  nvcc (grid <-> network resampling, warm-start initialisation)
   csrc/nn.cu         nvcc (layer kernels of the warm-start network, forward and backward)
+  csrc/nn_tc.cu      nvcc (its convolutions on the tensor cores: tcgen05, TMA, bf16 operands)
   csrc/postproc.cu   nvcc, -fmad=false (field3d, cut planes, streamlines in the reference's float64 order)
   csrc/prepare.cu    nvcc (duct, flood fill, leak, outlet, classes, kpad, segments, compact cell list)
   csrc/api.cpp       g++ -ffp-contract=off (host side of the C ABI)
@@ -36,6 +37,7 @@ UNITS = [
     ("lbm_fast.cu", []),
     ("warmstart.cu", []),
     ("nn.cu", []),
+    ("nn_tc.cu", []),
     ("postproc.cu", ["-fmad=false"]),
     ("prepare.cu", []),
     ("api.cpp", None),

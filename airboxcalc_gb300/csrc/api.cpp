@@ -1254,7 +1254,21 @@ extern "C" int abx_net_create(const abx_net_params *p, abx_net **out) {
   n->net.device = p->device;
   cudaError_t e = n->net.init(R, p->base, L, p->device, p->seed, p->coords != 0);
   if (e != cudaSuccess) return cuda_fail(e, "net_create");
+  // convolutions on the tensor cores with ABX_NN_TC=1 (default: the float32 kernels)
+  const char *tc = std::getenv("ABX_NN_TC");
+  n->net.use_tc = nn_tc_available() && tc && tc[0] == '1';
   *out = n.release();
+  return ABX_OK;
+}
+
+extern "C" int abx_net_set_tensor_cores(abx_net *n, int on) {
+  clear_stale_error();
+  if (!n) return fail(ABX_ERR_INVALID_ARGUMENT, "net_set_tensor_cores: null network");
+  CK(cudaSetDevice(n->net.device), "net_set_tensor_cores");
+  if (on && !nn_tc_available()) return fail(ABX_ERR_INVALID_ARGUMENT, "net_set_tensor_cores: this GPU has no tcgen05 tensor cores");
+  CK(cudaStreamSynchronize(n->net.st), "net_set_tensor_cores");
+  n->net.use_tc = on != 0;
+  if (!on) n->net.tc_free();
   return ABX_OK;
 }
 
@@ -1266,6 +1280,7 @@ extern "C" int abx_net_get_info(const abx_net *n, abx_net_info *o) {
   o->res = n->net.R; o->base = n->net.base; o->levels = n->net.levels;
   o->in_channels = n->net.n_in; o->out_channels = WarmNet::kOut;
   o->n_samples = (int)n->net.samples.size(); o->n_params = n->net.n_params;
+  o->tensor_cores = n->net.use_tc ? 1 : 0;
   return ABX_OK;
 }
 

@@ -3,6 +3,7 @@
 // beyond the runtime's stream type.
 #pragma once
 #include <cuda_runtime_api.h>
+#include <cuda_bf16.h>
 #include <vector_types.h>
 #include <stdint.h>
 
@@ -290,6 +291,31 @@ cudaError_t nn_conv3d_backward(const float *x, const float *w, const float *y, f
                                float *db, float *part, int64_t part_floats, int B, int Cin, int Cout, int D, int H,
                                int W, int s, int relu, int accum_dx, cudaStream_t st);
 int64_t nn_wgrad_scratch_floats(int Cin, int Cout, int Vo);
+// The same convolutions on the tensor cores (nn_tc.cu; tcgen05, bf16 operands, float32 accumulation and float32
+// tensors in and out).  Scratch: a channels-last bf16 copy of a layer's input, its bf16 weight slices, three
+// shifted channels-first copies of the input and a channels-first copy of the output gradient (weight gradient),
+// and the weight-gradient partial sums; err receives 1 if a kernel gave up waiting.
+struct TcScratch {
+  __nv_bfloat16 *cl = nullptr, *w = nullptr, *xs = nullptr, *dyc = nullptr;
+  float *part = nullptr;
+  int64_t cl_elems = 0, w_elems = 0, xs_elems = 0, dyc_elems = 0, part_floats = 0;
+  int *err = nullptr;
+};
+struct TcNeed {
+  int64_t cl_elems = 0, w_elems = 0, xs_elems = 0, dyc_elems = 0, part_floats = 0;
+};
+// true on a GPU whose tensor cores these kernels drive (compute capability 10.x)
+bool nn_tc_available();
+// grow `n` to what one layer (B samples, Cin -> Cout, D^3 input, stride s) needs
+void nn_tc_need(int B, int Cin, int Cout, int D, int s, TcNeed *n);
+int tc_wgrad_splits();
+cudaError_t nn_tc_conv3d(const float *x, const float *w, const float *b, float *y, int B, int Cin, int Cout, int D, int H,
+                         int W, int s, int relu, int accum, const TcScratch &sc, cudaStream_t st);
+// as nn_conv3d_backward; part / part_floats: the float32 weight-gradient scratch for layers with rows under 16
+// voxels, which run on the float32 kernels
+cudaError_t nn_tc_conv3d_backward(const float *x, const float *w, const float *y, float *dy, float *dx, float *dw,
+                                  float *db, float *part, int64_t part_floats, int B, int Cin, int Cout, int D, int H,
+                                  int W, int s, int relu, int accum_dx, const TcScratch &sc, cudaStream_t st);
 cudaError_t nn_upsample2(const float *x, float *y, int64_t BC, int D, int H, int W, cudaStream_t st);
 cudaError_t nn_upsample2_backward(const float *dy, float *dx, int64_t BC, int D, int H, int W, int accum,
                                   cudaStream_t st);

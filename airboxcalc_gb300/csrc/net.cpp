@@ -25,6 +25,7 @@ static double uniform01(uint64_t &s) { return (double)(splitmix(s) >> 11) * (1.0
 
 WarmNet::~WarmNet() {
   cudaSetDevice(device);
+  tc_free();
   cudaFree(d_p); cudaFree(d_g); cudaFree(d_m); cudaFree(d_v);
   cudaFree(d_act); cudaFree(d_grad); cudaFree(d_bt); cudaFree(d_bm); cudaFree(d_part);
   cudaFree(d_mse); cudaFree(d_seed);
@@ -108,6 +109,34 @@ cudaError_t WarmNet::init(int R_, int base_, int levels_, int device_, uint64_t 
   return cudaSuccess;
 }
 
+void WarmNet::tc_free() {
+  cudaFree(tcs.cl); cudaFree(tcs.w); cudaFree(tcs.xs); cudaFree(tcs.dyc); cudaFree(tcs.part); cudaFree(tcs.err);
+  tcs = TcScratch{};
+  tcs_B = 0;
+}
+
+cudaError_t WarmNet::tc_alloc(int B) {
+  if (tcs_B >= B) return cudaSuccess;
+  tc_free();
+  TcNeed need;
+  for (const Node &n : nodes)
+    if (n.kind == 0 && tc_layer(convs[n.conv])) {
+      const Conv &c = convs[n.conv];
+      nn_tc_need(B, c.cin, c.cout, tensors[n.in].D, c.stride, &need);
+    }
+  NCK(cudaMalloc((void **)&tcs.cl, 2 * std::max<int64_t>(need.cl_elems, 8)));
+  NCK(cudaMalloc((void **)&tcs.w, 2 * std::max<int64_t>(need.w_elems, 8)));
+  NCK(cudaMalloc((void **)&tcs.xs, 2 * std::max<int64_t>(need.xs_elems, 8)));
+  NCK(cudaMalloc((void **)&tcs.dyc, 2 * std::max<int64_t>(need.dyc_elems, 8)));
+  NCK(cudaMalloc((void **)&tcs.part, 4 * std::max<int64_t>(need.part_floats, 8)));
+  NCK(cudaMalloc((void **)&tcs.err, sizeof(int)));
+  NCK(cudaMemsetAsync(tcs.err, 0, sizeof(int), st));
+  tcs.cl_elems = need.cl_elems; tcs.w_elems = need.w_elems; tcs.xs_elems = need.xs_elems;
+  tcs.dyc_elems = need.dyc_elems; tcs.part_floats = need.part_floats;
+  tcs_B = B;
+  return cudaSuccess;
+}
+
 cudaError_t WarmNet::ensure_batch(int B) {
   if (B <= cap_B) return cudaSuccess;
   NCK(cudaSetDevice(device));
@@ -124,12 +153,17 @@ cudaError_t WarmNet::ensure_batch(int B) {
 }
 
 cudaError_t WarmNet::forward(int B) {
+  if (use_tc) NCK(tc_alloc(cap_B));
   for (const Node &n : nodes) {
     const Tensor &ti = tensors[n.in];
     if (n.kind == 0) {
       const Conv &c = convs[n.conv];
-      NCK(nn_conv3d(tensor(n.in), d_p + c.w_off, d_p + c.b_off, tensor(n.out), B, c.cin, c.cout, ti.D, ti.D, ti.D,
-                    c.stride, c.relu, 0, st));
+      if (tc_layer(c))
+        NCK(nn_tc_conv3d(tensor(n.in), d_p + c.w_off, d_p + c.b_off, tensor(n.out), B, c.cin, c.cout, ti.D, ti.D, ti.D,
+                         c.stride, c.relu, 0, tcs, st));
+      else
+        NCK(nn_conv3d(tensor(n.in), d_p + c.w_off, d_p + c.b_off, tensor(n.out), B, c.cin, c.cout, ti.D, ti.D, ti.D,
+                      c.stride, c.relu, 0, st));
     } else if (n.kind == 1) {
       const int D = tensors[n.out].D;
       NCK(nn_upsample2(tensor(n.in), tensor(n.out), (int64_t)B * ti.C, D, D, D, st));
@@ -154,9 +188,14 @@ cudaError_t WarmNet::loss(int B, const float *t, const float *m, double scale, b
       const Tensor &ti = tensors[n.in];
       if (n.kind == 0) {
         const Conv &c = convs[n.conv];
-        NCK(nn_conv3d_backward(tensor(n.in), d_p + c.w_off, tensor(n.out), grad(n.out), n.in == 0 ? nullptr : grad(n.in),
-                               d_g + c.w_off, d_g + c.b_off, d_part, part_floats, B, c.cin, c.cout, ti.D, ti.D, ti.D,
-                               c.stride, c.relu, 1, st));
+        if (tc_layer(c))
+          NCK(nn_tc_conv3d_backward(tensor(n.in), d_p + c.w_off, tensor(n.out), grad(n.out),
+                                    n.in == 0 ? nullptr : grad(n.in), d_g + c.w_off, d_g + c.b_off, d_part, part_floats,
+                                    B, c.cin, c.cout, ti.D, ti.D, ti.D, c.stride, c.relu, 1, tcs, st));
+        else
+          NCK(nn_conv3d_backward(tensor(n.in), d_p + c.w_off, tensor(n.out), grad(n.out), n.in == 0 ? nullptr : grad(n.in),
+                                 d_g + c.w_off, d_g + c.b_off, d_part, part_floats, B, c.cin, c.cout, ti.D, ti.D, ti.D,
+                                 c.stride, c.relu, 1, st));
       } else if (n.kind == 1) {
         NCK(nn_upsample2_backward(grad(n.out), grad(n.in), (int64_t)B * ti.C, ti.D, ti.D, ti.D, 1, st));
       } else {
@@ -167,6 +206,11 @@ cudaError_t WarmNet::loss(int B, const float *t, const float *m, double scale, b
     }
   }
   NCK(cudaStreamSynchronize(st));
+  if (use_tc && tcs.err) {
+    int e = 0;
+    NCK(cudaMemcpy(&e, tcs.err, sizeof e, cudaMemcpyDeviceToHost));
+    if (e) return cudaErrorLaunchTimeout;   // a tensor-core kernel gave up waiting for its copies
+  }
   double sum = 0;
   for (double v : part) sum += v;
   *out = sum;

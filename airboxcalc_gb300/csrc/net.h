@@ -49,6 +49,14 @@ class WarmNet {
   int *d_seed = nullptr;                              // 2 x R^3 jump-flood scratch
   std::vector<Sample> samples;
   std::string err;
+  // convolutions on the tensor cores (nn_tc.cu) where a layer's channels allow (<= 128 in and out), else the
+  // float32 kernels of nn.cu; tcs is sized for tcs_B samples
+  bool use_tc = false;
+  TcScratch tcs;
+  int tcs_B = 0;
+  bool tc_layer(const Conv &c) const { return use_tc && c.cin <= 128 && c.cout <= 128; }
+  cudaError_t tc_alloc(int B);
+  void tc_free();
 
   ~WarmNet();
   // Builds the layer list, allocates the parameters and initialises them from `seed`.

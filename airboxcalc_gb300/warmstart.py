@@ -63,6 +63,10 @@ class Net:
         E._check(A.load().abx_net_get_info(self._h, C.byref(i)))
         return {k: getattr(i, k) for k, _ in A.NetInfo._fields_}
 
+    def set_tensor_cores(self, on: bool = True):
+        """Convolutions on the tensor cores (tcgen05, bf16 operands) or on the float32 kernels."""
+        E._check(A.load().abx_net_set_tensor_cores(self._h, 1 if on else 0))
+
     @property
     def n_params(self) -> int:
         return self.info["n_params"]

@@ -25,7 +25,8 @@ extern "C" {
 
 /* Version of the structures and entry points below; a host compares it with abx_abi_version() before use.
  * 2: prepare timings in abx_geom_info, coordinate channels in abx_net_params, batch groups.
- * 3: abx_run_params.flags (bfloat16 storage only on request), vectorised-kernel fields in abx_sim_info. */
+ * 3: abx_run_params.flags (bfloat16 storage only on request), vectorised-kernel fields in abx_sim_info,
+ *    stop rules in abx_converge_params, tensor-core convolutions of the warm-start network. */
 #define ABX_ABI_VERSION 3
 
 /* Status codes.  The first group mirrors the errors engine.js throws. */
@@ -313,9 +314,14 @@ typedef struct {
 typedef struct {
   int res, base, levels, in_channels, out_channels, n_samples;
   long long n_params;
+  int tensor_cores;         /* 1: convolutions of up to 128 channels run on the tensor cores (tcgen05, bf16
+                               operands, float32 accumulation); 0: all on the float32 kernels */
 } abx_net_info;
 
 int abx_net_create(const abx_net_params *p, abx_net **out);
+/* Convolutions on the tensor cores (on; where the GPU has tcgen05 tensor cores) or all on the
+ * float32 kernels (off).  No counterpart in the reference. */
+int abx_net_set_tensor_cores(abx_net *n, int on);
 void abx_net_free(abx_net *n);
 int abx_net_get_info(const abx_net *n, abx_net_info *out);
 /* All weights and biases, n_params floats (layer by layer, weights

@@ -34,10 +34,20 @@ def _torch():
     return torch
 
 
-@pytest.mark.parametrize("res,base,levels,coords", [(8, 8, 2, False), (16, 8, 3, False), (8, 8, 2, True)])
-def test_network_gradients_match_torch_autograd(res, base, levels, coords):
+# float32 convolutions: to float32 rounding; tensor cores (bf16 operands, float32 accumulation): to bf16 rounding
+# (8 significant bits of every operand, a few per mille per layer, compounding through the layers)
+TOL = {False: dict(pred=1e-4, loss=1e-5, grad=1e-4), True: dict(pred=3e-2, loss=3e-2, grad=6e-2)}
+
+
+@pytest.mark.parametrize("tc", [False, True])
+@pytest.mark.parametrize("res,base,levels,coords", [(8, 8, 2, False), (16, 8, 3, False), (8, 8, 2, True),
+                                                    (32, 8, 2, False)])
+def test_network_gradients_match_torch_autograd(res, base, levels, coords, tc):
     torch = _torch()
     net = W.Net(res, base, levels, seed=3, coords=coords)
+    net.set_tensor_cores(tc)
+    assert net.info["tensor_cores"] == int(tc)
+    tol = TOL[tc]
     w = net.get_weights()
     assert w.size == net.n_params and net.info["in_channels"] == net.n_in
     rng = np.random.default_rng(1)
@@ -60,15 +70,15 @@ def test_network_gradients_match_torch_autograd(res, base, levels, coords):
     L = scale * (M[:, None] * (P - T) ** 2).sum()
     L.backward()
     ref_pred = P.detach().numpy()
-    assert np.abs(pred - ref_pred).max() <= 1e-4 * np.abs(ref_pred).max()
-    assert abs(loss - L.item()) <= 1e-5 * abs(L.item())
+    assert np.abs(pred - ref_pred).max() <= tol["pred"] * np.abs(ref_pred).max()
+    assert abs(loss - L.item()) <= tol["loss"] * abs(L.item())
     off = 0
     for i, (wt, bs, s, relu) in enumerate(layers):
         for ref in (wt.grad.numpy().ravel(), bs.grad.numpy().ravel()):
             got = grad[off:off + ref.size]
             off += ref.size
             err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
-            assert err < 1e-4, f"layer {i}: relative gradient error {err:.2e}"
+            assert err < tol["grad"], f"layer {i}: relative gradient error {err:.2e}"
     assert off == grad.size
 
 
