@@ -1254,9 +1254,9 @@ extern "C" int abx_net_create(const abx_net_params *p, abx_net **out) {
   n->net.device = p->device;
   cudaError_t e = n->net.init(R, p->base, L, p->device, p->seed, p->coords != 0);
   if (e != cudaSuccess) return cuda_fail(e, "net_create");
-  // convolutions on the tensor cores with ABX_NN_TC=1 (default: the float32 kernels)
+  // convolutions on the tensor cores where the GPU has them, unless ABX_NN_TC=0
   const char *tc = std::getenv("ABX_NN_TC");
-  n->net.use_tc = nn_tc_available() && tc && tc[0] == '1';
+  n->net.use_tc = nn_tc_available() && !(tc && tc[0] == '0');
   *out = n.release();
   return ABX_OK;
 }

@@ -257,15 +257,19 @@ struct WgradArgs {
   int bw;                // voxels of one K-step (a row segment): Wo, at most 64
   int arows, brows;      // rows of the A and B boxes (Cout, min(Cin, N)); the tiles' other rows feed only
                          // accumulator rows and columns that are not stored
+  int abytes, stage;     // bytes of a stage's A region (Cout rows, whole 1024-byte swizzle atoms) and of a stage
   int rows;              // K-steps in all: B * Do * Ho * (Wo / bw)
   int per;               // K-steps per CTA
   int *err;
 };
+// A stage holds the Cout rows of A and the N rows of B.  The MMA (M = 128) reads 128 rows of A from the stage's
+// start; the rows past Cout are whatever follows in shared memory (this stage's B, the next stage), which feeds
+// only accumulator rows that are not stored, and the last stage is followed by 128 rows of slack.
 template <int ROW, int N, int STAGES>
 struct WgradCfg {
-  static constexpr int kA = 128 * ROW, kB = N * ROW;
-  static constexpr int kStage = (kA + kB + 1023) / 1024 * 1024;
-  static constexpr int kSmem = STAGES * kStage + 1024;
+  static constexpr int kSlack = 128 * ROW + 1024;   // + alignment
+  static int stage_bytes(int abytes) { return (abytes + N * ROW + 1023) / 1024 * 1024; }
+  static int smem(int abytes) { return STAGES * stage_bytes(abytes) + kSlack; }
 };
 
 // grid (27, nsplit); mapDY: channels-first dY {Wo, Ho, Do, Cout, B}, box {bw, 1, 1, Cout, 1}; mapXk: the input
@@ -275,7 +279,6 @@ __global__ void __launch_bounds__(128, 1) conv_wgrad_kernel(const __grid_constan
                                                             const __grid_constant__ CUtensorMap mapX0,
                                                             const __grid_constant__ CUtensorMap mapX1,
                                                             const __grid_constant__ CUtensorMap mapX2, const WgradArgs p) {
-  using C = WgradCfg<ROW, N, STAGES>;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long full[STAGES], empty[STAGES], accf;
   __shared__ uint32_t tmem_base;
@@ -306,7 +309,7 @@ __global__ void __launch_bounds__(128, 1) conv_wgrad_kernel(const __grid_constan
       if (use > 0 && !mbar_wait(saddr(&empty[s]), (use - 1) & 1)) { fail = 1; break; }
       const int r = k0 + k;                     // (b, oz, oy, x-chunk) of the K-step
       const int xc = r % nwb, oy = (r / nwb) % p.Ho, oz = (r / (nwb * p.Ho)) % p.Do, b = r / (nwb * p.Ho * p.Do);
-      const uint32_t a = saddr(smem + s * C::kStage), bb = a + C::kA, bar = saddr(&full[s]);
+      const uint32_t a = saddr(smem + s * p.stage), bb = a + p.abytes, bar = saddr(&full[s]);
       mbar_expect_tx(bar, (uint32_t)((p.arows + p.brows) * ROW));
       tma_load_5d(a, &mapDY, xc * p.bw, oy, oz, 0, b, bar);
       tma_load_5d(bb, mapX, xc * p.bw, oy * p.s + ky - 1, oz * p.s + kz - 1, 0, b, bar);
@@ -321,7 +324,7 @@ __global__ void __launch_bounds__(128, 1) conv_wgrad_kernel(const __grid_constan
       const int s = k % STAGES;
       if (!mbar_wait(saddr(&full[s]), (k / STAGES) & 1)) { ok = false; break; }
       tc_fence_after();
-      const uint32_t a = saddr(smem + s * C::kStage), bb = a + C::kA;
+      const uint32_t a = saddr(smem + s * p.stage), bb = a + p.abytes;
 #pragma unroll
       for (int j = 0; j < ROW / 32; j++)
         mma_bf16(tmem, smem_desc(a + 32 * j, ROW), smem_desc(bb + 32 * j, ROW), id, (k > 0 || j > 0) ? 1u : 0u);
@@ -436,20 +439,32 @@ __global__ void wgrad_sum_kernel(const float *__restrict__ part, float *__restri
   }
 }
 
-// db[co] = sum over samples and voxels of dy[b][co][v]; one block of 256 threads per channel, fixed order
-__global__ void bias_grad_kernel(const float *__restrict__ dy, float *__restrict__ db, int B, int Cout, int64_t V) {
+// db[co] = sum over samples and voxels of dy[b][co][v], in two fixed-order passes: grid (kBiasParts, Cout) blocks
+// of 256 threads each sum a slice of the channel into part[co][slice]; then one thread per channel adds the slices.
+constexpr int kBiasParts = 64;
+__global__ void bias_part_kernel(const float *__restrict__ dy, float *__restrict__ part, int B, int Cout, int64_t V) {
   __shared__ float red[256];
-  const int co = blockIdx.x;
+  const int co = blockIdx.y, sl = blockIdx.x;
+  const int64_t n = (int64_t)B * V, lo = n * sl / kBiasParts, hi = n * (sl + 1) / kBiasParts;
   float t = 0.0f;
-  for (int b = 0; b < B; b++)
-    for (int64_t v = threadIdx.x; v < V; v += blockDim.x) t += dy[((int64_t)b * Cout + co) * V + v];
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const int64_t b = i / V, v = i % V;
+    t += dy[((int64_t)b * Cout + co) * V + v];
+  }
   red[threadIdx.x] = t;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
     if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) db[co] = red[0];
+  if (threadIdx.x == 0) part[co * kBiasParts + sl] = red[0];
+}
+__global__ void bias_sum_kernel(const float *__restrict__ part, float *__restrict__ db, int Cout) {
+  const int co = blockIdx.x * blockDim.x + threadIdx.x;
+  if (co >= Cout) return;
+  float t = 0.0f;
+  for (int sl = 0; sl < kBiasParts; sl++) t += part[co * kBiasParts + sl];
+  db[co] = t;
 }
 
 __global__ void relu_mask_kernel(const float *__restrict__ y, float *__restrict__ dy, int64_t n) {
@@ -499,6 +514,11 @@ static int k_row(int cp) { return cp == 16 ? 32 : cp == 32 ? 64 : 128; }
 static int n_pad(int c) { return c <= 16 ? 16 : c <= 32 ? 32 : c <= 64 ? 64 : 128; }
 
 constexpr int kStages = 4;
+// pipeline depth of the weight-gradient kernel (its stages are small: one row of voxels each)
+#ifndef ABX_TC_WSTAGES
+#define ABX_TC_WSTAGES 4
+#endif
+constexpr int kWStages = ABX_TC_WSTAGES;
 
 template <int ROW, int N>
 static cudaError_t launch_fwd(const CUtensorMap &mx, const CUtensorMap &mw, const FwdArgs &a, dim3 grid, cudaStream_t st) {
@@ -527,15 +547,18 @@ static cudaError_t launch_fwd_n(int N, const CUtensorMap &mx, const CUtensorMap 
 template <int ROW, int N>
 static cudaError_t launch_wgrad(const CUtensorMap &mdy, const CUtensorMap *mx, const WgradArgs &a, dim3 grid,
                                 cudaStream_t st) {
-  constexpr int smem = WgradCfg<ROW, N, kStages>::kSmem;
-  static bool attr = false;
-  if (!attr) {
+  using C = WgradCfg<ROW, N, kWStages>;
+  const int smem = C::smem(a.abytes);
+  static int attr = 0;   // the largest dynamic shared memory set so far for this instantiation
+  if (smem > attr) {
     cudaError_t e =
-        cudaFuncSetAttribute(conv_wgrad_kernel<ROW, N, kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(conv_wgrad_kernel<ROW, N, kWStages>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    attr = true;
+    attr = smem;
   }
-  conv_wgrad_kernel<ROW, N, kStages><<<grid, 128, smem, st>>>(mdy, mx[0], mx[1], mx[2], a);
+  WgradArgs b = a;
+  b.stage = C::stage_bytes(a.abytes);
+  conv_wgrad_kernel<ROW, N, kWStages><<<grid, 128, smem, st>>>(mdy, mx[0], mx[1], mx[2], b);
   return cudaGetLastError();
 }
 template <int ROW>
@@ -608,7 +631,10 @@ bool nn_tc_available() {
   return major == 10 && tc::encoder() != nullptr;
 }
 
-int tc_wgrad_splits() { return 48; }
+#ifndef ABX_TC_WSPLITS
+#define ABX_TC_WSPLITS 48
+#endif
+int tc_wgrad_splits() { return ABX_TC_WSPLITS; }
 
 void nn_tc_need(int B, int Cin, int Cout, int D, int s, TcNeed *n) {
   const int64_t V = (int64_t)D * D * D;
@@ -619,7 +645,7 @@ void nn_tc_need(int B, int Cin, int Cout, int D, int s, TcNeed *n) {
   n->w_elems = std::max(n->w_elems, (int64_t)27 * std::max(tc::n_pad(Cout) * kf, tc::n_pad(Cin) * kb));
   n->xs_elems = std::max(n->xs_elems, (int64_t)3 * B * Cin * D * D * Do);
   n->dyc_elems = std::max(n->dyc_elems, (int64_t)B * Cout * Vo);
-  n->part_floats = std::max(n->part_floats, (int64_t)tc_wgrad_splits() * 27 * Cout * Cin);
+  n->part_floats = std::max(n->part_floats, (int64_t)std::max(tc_wgrad_splits() * 27 * Cin, tc::kBiasParts) * Cout);
 }
 
 cudaError_t nn_tc_conv3d(const float *x, const float *w, const float *b, float *y, int B, int Cin, int Cout, int D, int H,
@@ -669,6 +695,7 @@ cudaError_t nn_tc_conv3d_backward(const float *x, const float *w, const float *y
     tc::WgradArgs a{};
     a.part = sc.part; a.Cout = Cout; a.Cin = Cin; a.Do = Do; a.Ho = Ho; a.Wo = Wo; a.s = s; a.bw = bw;
     a.arows = Cout; a.brows = std::min(Cin, N);
+    a.abytes = (Cout * row + 1023) / 1024 * 1024;
     a.rows = B * Do * Ho * (Wo / bw);
     const int nsplit = std::min(tc_wgrad_splits(), a.rows);
     a.per = (a.rows + nsplit - 1) / nsplit;
@@ -684,7 +711,9 @@ cudaError_t nn_tc_conv3d_backward(const float *x, const float *w, const float *y
     }
     if (e != cudaSuccess) return e;
     tc::wgrad_sum_kernel<<<tc::blocks_for((int64_t)Cout * Cin * 27), 256, 0, st>>>(sc.part, dw, Cout, Cin, nsplit);
-    tc::bias_grad_kernel<<<Cout, 256, 0, st>>>(dy, db, B, Cout, Vo);
+    // the bias partials reuse the weight-gradient scratch after the sums above have read it (same stream)
+    tc::bias_part_kernel<<<dim3(tc::kBiasParts, Cout), 256, 0, st>>>(dy, sc.part, B, Cout, Vo);
+    tc::bias_sum_kernel<<<(Cout + 127) / 128, 128, 0, st>>>(sc.part, db, Cout);
     return cudaGetLastError();
   }
   // rows narrower than 16 voxels: the float32 kernels (the ReLU mask is already applied)

@@ -485,6 +485,64 @@ def batch_variants(n: int, seed0: int = 7000):
     return out
 
 
+def net_flops(res: int, base: int, levels: int, batch: int) -> float:
+    """Multiply-add FLOPs (2 per MAC) of one training step of the warm-start network: every convolution's
+    forward, data gradient (all but the first layer's) and weight gradient."""
+    chans = [base << l for l in range(levels)]
+    conv, d, c = [], res, 9
+    for l in range(levels):
+        d = d if l == 0 else d // 2
+        conv += [(c, chans[l], d), (chans[l], chans[l], d)]
+        c = chans[l]
+    for l in range(levels - 2, -1, -1):
+        d *= 2
+        conv += [(chans[l + 1], chans[l], d), (chans[l], chans[l], d)]
+    conv.append((chans[0], 4, d))
+    total = 0.0
+    for i, (cin, cout, do) in enumerate(conv):
+        f = 2.0 * 27 * cin * cout * do ** 3 * batch
+        total += f * (2 if i == 0 else 3)
+    return total
+
+
+def study_net(batch: int = 8, iters: int = 10, modes=("f32", "tc"), res: int = 64, base: int = 16, levels: int = 4):
+    """One training step (forward, loss, backward) of the warm-start network at its shipped shape on synthetic
+    inputs, timed per convolution path: the float32 kernels and the tensor cores (bf16 operands, float32
+    accumulation).  Reports ms per step and TFLOP/s of the convolutions' multiply-adds."""
+    import torch
+    from airboxcalc_gb300 import warmstart as W
+    rng = np.random.default_rng(0)
+    flops = net_flops(res, base, levels, batch)
+    out = {"study": "net", "res": res, "base": base, "levels": levels, "batch": batch, "iters": iters,
+           "tflop_per_step": round(flops / 1e12, 4)}
+    for mode in modes:
+        net = W.Net(res, base, levels, seed=3)
+        net.set_tensor_cores(mode == "tc")
+        x = torch.from_numpy(rng.standard_normal((batch, net.n_in, res, res, res)).astype(np.float32)).cuda()
+        t = torch.from_numpy(rng.standard_normal((batch, 4, res, res, res)).astype(np.float32)).cuda()
+        m = torch.ones((batch, res, res, res), dtype=torch.float32, device="cuda")
+        pred = torch.empty((batch, 4, res, res, res), dtype=torch.float32, device="cuda")
+        grad = torch.empty(net.n_params, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+
+        def step():
+            return net.forward_backward(x.data_ptr(), t.data_ptr(), m.data_ptr(), batch, 1.0 / m.numel(),
+                                        pred.data_ptr(), grad.data_ptr())
+
+        step()
+        t0 = time.perf_counter()
+        for _ in range(iters):
+            step()
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) / iters * 1e3
+        out[mode] = {"ms_per_step": round(ms, 3), "tflops": round(flops / ms / 1e9, 1)}
+        del net
+    if "f32" in out and "tc" in out:
+        out["speedup"] = round(out["f32"]["ms_per_step"] / out["tc"]["ms_per_step"], 2)
+    print(json.dumps(out), flush=True)
+    return out
+
+
 def study_batch(n: int = 64, storage: str = "f16", quiet: bool = False):
     """Batched variants: every seeded airbox alone in float32 (the reference's method, one solve at a
     time), alone in `storage`, and all together in one batched run (tuned shape, one launch per step).
@@ -626,10 +684,15 @@ def main():
     ap.add_argument("--e2e-solves", type=int, default=2, help="whole end-to-end solves timed for e2e")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-warm-start", action="store_true", help="skip the warm-start sample of the bench line")
-    ap.add_argument("--study", choices=["precision", "converge", "warmstart", "batch", "decorrelation"], default=None,
+    ap.add_argument("--study", choices=["precision", "converge", "warmstart", "batch", "decorrelation", "net"],
+                    default=None,
                     help="instead of the bench line: KPI error per storage vs float64, steps/time to converged "
-                         "KPIs, the learned warm start on held-out airboxes, the batched variant table, or the "
-                         "growth of the float32/float16 vs float64 field difference over a solve")
+                         "KPIs, the learned warm start on held-out airboxes, the batched variant table, the "
+                         "growth of the float32/float16 vs float64 field difference over a solve, or one "
+                         "training step of the warm-start network on the float32 kernels and the tensor cores")
+    ap.add_argument("--net-batch", type=int, default=8, help="batch of --study net")
+    ap.add_argument("--net-iters", type=int, default=10, help="timed training steps of --study net")
+    ap.add_argument("--net-modes", default="f32,tc", help="convolution paths of --study net")
     ap.add_argument("--seeds", default="6000:6200", help="held-out seed range a:b of --study warmstart")
     ap.add_argument("--storages", default="f64,f32exact,f32,f16,bf16", help="storages of --study precision")
     ap.add_argument("--weights", default=None, help="warm-start network weights (.npz)")
@@ -647,6 +710,9 @@ def main():
         return 0
     if a.study == "batch":
         study_batch(64, "f16")
+        return 0
+    if a.study == "net":
+        study_net(a.net_batch, a.net_iters, tuple(a.net_modes.split(",")))
         return 0
     if a.study == "warmstart":
         from airboxcalc_gb300 import warmstart as W

@@ -320,7 +320,8 @@ typedef struct {
 
 int abx_net_create(const abx_net_params *p, abx_net **out);
 /* Convolutions on the tensor cores (on; where the GPU has tcgen05 tensor cores) or all on the
- * float32 kernels (off).  No counterpart in the reference. */
+ * float32 kernels (off).  A new network starts on the tensor cores where the GPU has them, unless
+ * the environment sets ABX_NN_TC=0.  No counterpart in the reference. */
 int abx_net_set_tensor_cores(abx_net *n, int on);
 void abx_net_free(abx_net *n);
 int abx_net_get_info(const abx_net *n, abx_net_info *out);

@@ -12,7 +12,10 @@ can be checked:
                   means), with an exact Euclidean distance transform where the
                   GPU uses jump flooding;
 * ``net_forward`` - the encoder-decoder in torch (CPU, float64), whose
-                  autograd gives the reference gradients;
+                  autograd gives the reference gradients; with
+                  ``bf16_operands`` every convolution rounds its operands to
+                  bfloat16 as the tensor-core kernels do (the sums stay
+                  float64), so that their gradients can be checked tightly;
 * ``apply``     - the warm start: trilinear interpolation of the prediction
                   weighted by voxel fluid fraction and the equilibrium of
                   cpuStep (src/engine.js:288-291).
@@ -157,14 +160,48 @@ def unpack(weights: np.ndarray, base: int, levels: int, torch, n_in: int = 9):
     return out
 
 
-def net_forward(layers, x, levels: int, torch):
+def _bf16_conv(torch):
+    """A 3x3x3 convolution (padding 1) that rounds its operands to bfloat16
+    the way the tensor-core path does: the forward rounds x and w; the data
+    gradient rounds the (ReLU-masked) output gradient and w; the weight
+    gradient rounds the output gradient and x where that path computes it on
+    the tensor cores (output rows of at least 16 voxels) and keeps float32
+    operands elsewhere; the bias gradient sums the unrounded output gradient."""
+    F = torch.nn.functional
+    G = torch.nn.grad
+
+    def r(t):
+        return t.to(torch.float32).to(torch.bfloat16).to(t.dtype)
+
+    class Bf16Conv(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, x, w, b, s):
+            xr, wr = r(x), r(w)
+            ctx.save_for_backward(x, xr, w, wr)
+            ctx.s = s
+            return F.conv3d(xr, wr, b, stride=s, padding=1)
+
+        @staticmethod
+        def backward(ctx, dy):
+            x, xr, w, wr = ctx.saved_tensors
+            s, dyr = ctx.s, r(dy)
+            dx = G.conv3d_input(x.shape, wr, dyr, stride=s, padding=1)
+            tc = dy.shape[-1] >= 16
+            dw = G.conv3d_weight(xr if tc else x, w.shape, dyr if tc else dy, stride=s, padding=1)
+            return dx, dw, dy.sum(dim=(0, 2, 3, 4)), None
+
+    return Bf16Conv.apply
+
+
+def net_forward(layers, x, levels: int, torch, bf16_operands: bool = False):
     """The encoder-decoder of the warm start (x: (B, 9 or 12, R, R, R) float64)."""
     F = torch.nn.functional
     it = iter(layers)
+    conv3d = _bf16_conv(torch) if bf16_operands else None
 
     def conv(t):
         w, b, s, relu = next(it)
-        y = F.conv3d(t, w, b, stride=s, padding=1)
+        y = conv3d(t, w, b, s) if bf16_operands else F.conv3d(t, w, b, stride=s, padding=1)
         return F.relu(y) if relu else y
 
     skips, t = [], x

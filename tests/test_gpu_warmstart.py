@@ -34,10 +34,20 @@ def _torch():
     return torch
 
 
-# float32 convolutions: to float32 rounding; tensor cores (bf16 operands, float32 accumulation): to bf16 rounding
-# (8 significant bits of every operand, a few per mille per layer, compounding through the layers)
-TOL = {False: dict(pred=1e-4, loss=1e-5, grad=1e-4), True: dict(pred=3e-2, loss=3e-2, grad=6e-2)}
-
+# float32 convolutions: against the float64 network, to float32 rounding.
+#
+# Tensor cores (bf16 operands, float32 accumulation): each convolution is exact to float32 summation error when its
+# operands are bf16 values (tests/native/conv_tc_check.cu, through test_gpu_conv_tc.py).  Through the whole network
+# no tight bound exists: a float32 sum that lands within its rounding error of a bf16 rounding boundary rounds the
+# other way than the float64 sum does (one bf16 unit, 0.4 %), the change spreads to the next layers' sums and tips
+# more of them, and pre-activations near zero then cross the ReLU, which switches whole gradient entries on or off.
+# Depending on the data this stays at float32 level or reaches a few per mille in the prediction and a few
+# per cent in a layer's parameter gradient (measured on six seeds at 8^3 to 16^3).  So the prediction and loss
+# are checked against the exact network to bf16 rounding, and the gradients against the network whose
+# convolutions round the same operands to bf16 (which removes the systematic part): every tensor within 15 %
+# relative L2 and the whole gradient within 5 %; a missing term of the backward pass (a skip connection, a mask,
+# an accumulation) is an error of order one.
+TOL = {False: dict(pred=1e-4, loss=1e-5, grad=1e-4), True: dict(pred=3e-2, loss=3e-2, grad=0.15, grad_all=0.05)}
 
 @pytest.mark.parametrize("tc", [False, True])
 @pytest.mark.parametrize("res,base,levels,coords", [(8, 8, 2, False), (16, 8, 3, False), (8, 8, 2, True),
@@ -64,22 +74,27 @@ def test_network_gradients_match_torch_autograd(res, base, levels, coords, tc):
                                 dgrad.data_ptr())
     pred, grad = dpred.cpu().numpy(), dgrad.cpu().numpy()
 
-    layers = R_.unpack(w, base, levels, torch, net.n_in)
     X, T, M = (torch.tensor(a, dtype=torch.float64) for a in (x, t, m))
-    P = R_.net_forward(layers, X, levels, torch)
+    with torch.no_grad():
+        P = R_.net_forward(R_.unpack(w, base, levels, torch, net.n_in), X, levels, torch)
+        L = scale * (M[:, None] * (P - T) ** 2).sum()
+    assert np.abs(pred - P.numpy()).max() <= tol["pred"] * np.abs(P.numpy()).max()
+    assert abs(loss - L.item()) <= tol["loss"] * abs(L.item())
+    layers = R_.unpack(w, base, levels, torch, net.n_in)
+    P = R_.net_forward(layers, X, levels, torch, bf16_operands=tc)
     L = scale * (M[:, None] * (P - T) ** 2).sum()
     L.backward()
-    ref_pred = P.detach().numpy()
-    assert np.abs(pred - ref_pred).max() <= tol["pred"] * np.abs(ref_pred).max()
-    assert abs(loss - L.item()) <= tol["loss"] * abs(L.item())
-    off = 0
+    off, refs = 0, []
     for i, (wt, bs, s, relu) in enumerate(layers):
         for ref in (wt.grad.numpy().ravel(), bs.grad.numpy().ravel()):
             got = grad[off:off + ref.size]
             off += ref.size
+            refs.append(ref)
             err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
             assert err < tol["grad"], f"layer {i}: relative gradient error {err:.2e}"
     assert off == grad.size
+    ref = np.concatenate(refs)
+    assert np.linalg.norm(grad - ref) / np.linalg.norm(ref) < tol.get("grad_all", tol["grad"])
 
 
 @pytest.mark.parametrize("coords", [False, True])
