@@ -274,6 +274,9 @@ struct WgradCfg {
 
 // grid (27, nsplit); mapDY: channels-first dY {Wo, Ho, Do, Cout, B}, box {bw, 1, 1, Cout, 1}; mapXk: the input
 // copy for tap column k, shifted by k - 1 along W and decimated by s: {Wo, H, D, Cin, B}, box {bw, 1, 1, brows, 1}.
+// Each channel's box row is one K-major operand row of bw voxels (bw * 2 bytes = the swizzle span).  Rows of 8
+// voxels are not stacked into one K-step: a box of several 16-byte rows per channel does not land as one dense
+// operand row under the 128-byte swizzle (tried: wrong sums, and the largest such box wrote past the stage).
 template <int ROW, int N, int STAGES>
 __global__ void __launch_bounds__(128, 1) conv_wgrad_kernel(const __grid_constant__ CUtensorMap mapDY,
                                                             const __grid_constant__ CUtensorMap mapX0,
@@ -363,27 +366,29 @@ __global__ void __launch_bounds__(128, 1) conv_wgrad_kernel(const __grid_constan
 // ------------------------------------------------------------------ layout conversions
 // x [B][C][D][H][W] float32 -> [B][D][H][W][Cp] bf16, channels >= C zero.  up2: the gradient of a stride-2
 // convolution zero-inserted to the input's size: voxel q holds x[q / 2] where every coordinate of q is even, zero
-// elsewhere (x is then a D/2 x H/2 x W/2 grid).
-__global__ void to_cl_kernel(const float *__restrict__ x, __nv_bfloat16 *__restrict__ out, int B, int C, int Cp, int D,
+// elsewhere (x is then a D/2 x H/2 x W/2 grid).  Grid (voxel blocks, B); voxel indices within a sample are 32-bit
+// (the host checks D * H * W < 2^31).
+__global__ void to_cl_kernel(const float *__restrict__ x, __nv_bfloat16 *__restrict__ out, int C, int Cp, int D,
                              int H, int W, int up2) {
   const int Dx = up2 ? D / 2 : D, Hx = up2 ? H / 2 : H, Wx = up2 ? W / 2 : W;
-  const int64_t Vx = (int64_t)Dx * Hx * Wx, V = (int64_t)D * H * W, n = (int64_t)B * V;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = i / V, v = i % V;
-    const int w = (int)(v % W), h = (int)((v / W) % H), d = (int)(v / ((int64_t)W * H));
+  const uint32_t Vx = (uint32_t)Dx * Hx * Wx, V = (uint32_t)D * H * W, HW = (uint32_t)H * W;
+  const float *xb = x + (int64_t)blockIdx.y * C * Vx;
+  __nv_bfloat16 *ob = out + (int64_t)blockIdx.y * V * Cp;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const uint32_t w = v % (uint32_t)W, h = (v / (uint32_t)W) % (uint32_t)H, d = v / HW;
     bool on = true;
-    int64_t src = v;
+    uint32_t src = v;
     if (up2) {
       on = !(w & 1) && !(h & 1) && !(d & 1);
-      src = ((int64_t)(d >> 1) * Hx + (h >> 1)) * Wx + (w >> 1);
+      src = ((d >> 1) * (uint32_t)Hx + (h >> 1)) * (uint32_t)Wx + (w >> 1);
     }
-    __nv_bfloat16 *o = out + i * Cp;
+    __nv_bfloat16 *o = ob + (size_t)v * Cp;
     for (int c0 = 0; c0 < Cp; c0 += 8) {
       __align__(16) __nv_bfloat16 q[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) {
         const int c = c0 + j;
-        q[j] = __float2bfloat16_rn((on && c < C) ? x[(b * C + c) * Vx + src] : 0.0f);
+        q[j] = __float2bfloat16_rn((on && c < C) ? xb[(size_t)c * Vx + src] : 0.0f);
       }
       *reinterpret_cast<uint4 *>(o + c0) = *reinterpret_cast<const uint4 *>(q);
     }
@@ -391,17 +396,20 @@ __global__ void to_cl_kernel(const float *__restrict__ x, __nv_bfloat16 *__restr
 }
 
 // x [B][C][D][H][W] float32 -> three bf16 copies [3][B][C][D][H][Wo]: copy kx holds x[..][s * w + kx - 1] (zero
-// outside the grid), Wo = (W - 1) / s + 1.
-__global__ void to_cf_shift_kernel(const float *__restrict__ x, __nv_bfloat16 *__restrict__ out, int64_t BCDH, int W,
-                                   int Wo, int s) {
-  const int64_t n = BCDH * Wo;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = i / Wo;
-    const int w = (int)(i % Wo);
+// outside the grid), Wo = (W - 1) / s + 1.  n = B * C * D * H * Wo (the copies' stride); grid (blocks, B), indices
+// within a sample 32-bit (the host checks C * D * H * W < 2^31).
+__global__ void to_cf_shift_kernel(const float *__restrict__ x, __nv_bfloat16 *__restrict__ out, int64_t n,
+                                   uint32_t rows, int W, int Wo, int s) {
+  const uint32_t m = rows * (uint32_t)Wo;   // one sample's elements per copy
+  const float *xb = x + (int64_t)blockIdx.y * rows * W;
+  __nv_bfloat16 *ob = out + (int64_t)blockIdx.y * m;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
+    const uint32_t r = j / (uint32_t)Wo, w = j % (uint32_t)Wo;
+    const float *xr = xb + (size_t)r * W;
 #pragma unroll
     for (int kx = 0; kx < 3; kx++) {
-      const int src = s * w + kx - 1;
-      out[kx * n + i] = __float2bfloat16_rn((src >= 0 && src < W) ? x[row * W + src] : 0.0f);
+      const int src = s * (int)w + kx - 1;
+      ob[kx * n + j] = __float2bfloat16_rn((src >= 0 && src < W) ? xr[src] : 0.0f);
     }
   }
 }
@@ -440,16 +448,17 @@ __global__ void wgrad_sum_kernel(const float *__restrict__ part, float *__restri
 }
 
 // db[co] = sum over samples and voxels of dy[b][co][v], in two fixed-order passes: grid (kBiasParts, Cout) blocks
-// of 256 threads each sum a slice of the channel into part[co][slice]; then one thread per channel adds the slices.
+// of 256 threads each sum one slice of the voxels over every sample into part[co][slice]; then one thread per channel
+// adds the slices.
 constexpr int kBiasParts = 64;
 __global__ void bias_part_kernel(const float *__restrict__ dy, float *__restrict__ part, int B, int Cout, int64_t V) {
   __shared__ float red[256];
   const int co = blockIdx.y, sl = blockIdx.x;
-  const int64_t n = (int64_t)B * V, lo = n * sl / kBiasParts, hi = n * (sl + 1) / kBiasParts;
+  const uint32_t lo = (uint32_t)(V * sl / kBiasParts), hi = (uint32_t)(V * (sl + 1) / kBiasParts);
   float t = 0.0f;
-  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-    const int64_t b = i / V, v = i % V;
-    t += dy[((int64_t)b * Cout + co) * V + v];
+  for (int b = 0; b < B; b++) {
+    const float *row = dy + ((int64_t)b * Cout + co) * V;
+    for (uint32_t v = lo + threadIdx.x; v < hi; v += blockDim.x) t += row[v];
   }
   red[threadIdx.x] = t;
   __syncthreads();
@@ -585,7 +594,8 @@ static cudaError_t conv_forward(const float *x, int Cin, bool up2, const float *
   // Cout_f = Cin (the gradient's input channels) and Cin_f = Cout; weights_kernel takes the forward's sizes
   weights_kernel<<<blocks_for((int64_t)27 * N * Kp), 256, 0, st>>>(w, sc.w, flip ? Cin : Cout, flip ? Cout : Cin, N, Kp,
                                                                   flip ? 1 : 0);
-  to_cl_kernel<<<blocks_for((int64_t)B * D * H * W), 256, 0, st>>>(x, sc.cl, B, Cin, Kp, D, H, W, up2 ? 1 : 0);
+  if ((int64_t)D * H * W >= (1ll << 31)) return cudaErrorInvalidValue;
+  to_cl_kernel<<<dim3(blocks_for((int64_t)D * H * W), (unsigned)B), 256, 0, st>>>(x, sc.cl, Cin, Kp, D, H, W, up2 ? 1 : 0);
   const int Do = (D - 1) / s + 1, Ho = (H - 1) / s + 1, Wo = (W - 1) / s + 1;
   FwdArgs a{};
   a.y = y; a.bias = bias; a.Cout = Cout; a.Do = Do; a.Ho = Ho; a.Wo = Wo; a.s = s;
@@ -650,14 +660,16 @@ void nn_tc_need(int B, int Cin, int Cout, int D, int s, TcNeed *n) {
 
 cudaError_t nn_tc_conv3d(const float *x, const float *w, const float *b, float *y, int B, int Cin, int Cout, int D, int H,
                          int W, int s, int relu, int accum, const TcScratch &sc, cudaStream_t st) {
-  if (B <= 0 || Cin <= 0 || Cout <= 0 || D <= 0 || H <= 0 || W <= 0 || (s != 1 && s != 2)) return cudaErrorInvalidValue;
+  if (B <= 0 || B > 65535 || Cin <= 0 || Cout <= 0 || D <= 0 || H <= 0 || W <= 0 || (s != 1 && s != 2))
+    return cudaErrorInvalidValue;
   return tc::conv_forward(x, Cin, false, w, false, b, y, B, Cout, D, H, W, s, relu, accum, sc, st);
 }
 
 cudaError_t nn_tc_conv3d_backward(const float *x, const float *w, const float *y, float *dy, float *dx, float *dw,
                                   float *db, float *part, int64_t part_floats, int B, int Cin, int Cout, int D, int H,
                                   int W, int s, int relu, int accum_dx, const TcScratch &sc, cudaStream_t st) {
-  if (B <= 0 || Cin <= 0 || Cout <= 0 || D <= 0 || H <= 0 || W <= 0 || (s != 1 && s != 2)) return cudaErrorInvalidValue;
+  if (B <= 0 || B > 65535 || Cin <= 0 || Cout <= 0 || D <= 0 || H <= 0 || W <= 0 || (s != 1 && s != 2))
+    return cudaErrorInvalidValue;
   if (s == 2 && ((D | H | W) & 1)) return cudaErrorInvalidValue;
   const int Do = (D - 1) / s + 1, Ho = (H - 1) / s + 1, Wo = (W - 1) / s + 1;
   const int64_t Vo = (int64_t)Do * Ho * Wo;
@@ -667,13 +679,16 @@ cudaError_t nn_tc_conv3d_backward(const float *x, const float *w, const float *y
     cudaError_t e = tc::conv_forward(dy, Cout, s == 2, w, true, nullptr, dx, B, Cin, D, H, W, 1, 0, accum_dx, sc, st);
     if (e != cudaSuccess) return e;
   }
-  // weight and bias gradients
-  if (Wo >= 16 && Cout <= 128) {
-    const int N = tc::n_pad(Cin), bw = std::min(Wo, 64), row = bw * 2;
+  // weight and bias gradients: K-steps of one row segment of 16, 32 or 64 voxels
+  const int bw = std::min(Wo, 64);
+  if (Cout <= 128 && (bw == 16 || bw == 32 || bw == 64) && Wo % bw == 0) {
+    const int N = tc::n_pad(Cin), row = bw * 2;
     if ((int64_t)3 * B * Cin * D * H * Wo > sc.xs_elems || (int64_t)B * Cout * Vo > sc.dyc_elems) return cudaErrorInvalidValue;
     tc::to_bf16_kernel<<<tc::blocks_for((int64_t)B * Cout * Vo), 256, 0, st>>>(dy, sc.dyc, (int64_t)B * Cout * Vo);
     const int64_t rows_x = (int64_t)B * Cin * D * H;
-    tc::to_cf_shift_kernel<<<tc::blocks_for(rows_x * Wo), 256, 0, st>>>(x, sc.xs, rows_x, W, Wo, s);
+    if ((int64_t)Cin * D * H * W >= (1ll << 31)) return cudaErrorInvalidValue;
+    tc::to_cf_shift_kernel<<<dim3(tc::blocks_for(rows_x / B * Wo), (unsigned)B), 256, 0, st>>>(
+        x, sc.xs, rows_x * Wo, (uint32_t)(rows_x / B), W, Wo, s);
     CUtensorMap mdy, mx[3];
     {
       const cuuint64_t dims[5] = {(cuuint64_t)Wo, (cuuint64_t)Ho, (cuuint64_t)Do, (cuuint64_t)Cout, (cuuint64_t)B};

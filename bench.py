@@ -325,6 +325,10 @@ def study_converge(spec, run, desc, storages=("f32", "f16", "bf16"), ladder=(600
 WARM_RULES = (dict(settle=1000, window=500, min_avg=1000, max_steps=4000, tol=0.01, rule=0, min_windows=4),
               dict(settle=500, window=250, min_avg=1000, max_steps=6000, tol=0.01, rule=1, min_windows=4),
               dict(settle=1000, window=500, min_avg=2000, max_steps=6000, tol=0.01, rule=1, min_windows=4))
+# Fixed step budgets (no stop test: a tolerance no window misses, two windows): settle S steps, then average A;
+# S + A = 1250, 1500, 2000 and 3000 steps, i.e. 4.8x, 4x, 3x and 2x fewer than the reference's 6000.
+BUDGET_RULES = tuple(dict(settle=s, window=a // 2, min_avg=a, max_steps=s + a, tol=1e9, rule=0, min_windows=2)
+                     for s, a in ((250, 1000), (500, 1000), (500, 1500), (1000, 2000)))
 
 
 def _rel_err(m, ref):
@@ -694,6 +698,9 @@ def main():
     ap.add_argument("--net-iters", type=int, default=10, help="timed training steps of --study net")
     ap.add_argument("--net-modes", default="f32,tc", help="convolution paths of --study net")
     ap.add_argument("--seeds", default="6000:6200", help="held-out seed range a:b of --study warmstart")
+    ap.add_argument("--warm-rules", default="stop", choices=["stop", "budget"],
+                    help="--study warmstart: the stop rules, or fixed step budgets (settle + average) without a stop "
+                         "test, which map the accuracy of the learned and of a perfect start against the budget")
     ap.add_argument("--storages", default="f64,f32exact,f32,f16,bf16", help="storages of --study precision")
     ap.add_argument("--weights", default=None, help="warm-start network weights (.npz)")
     a = ap.parse_args()
@@ -717,7 +724,10 @@ def main():
     if a.study == "warmstart":
         from airboxcalc_gb300 import warmstart as W
         lo, hi = map(int, a.seeds.split(":"))
-        study_warmstart(range(lo, hi), a.weights or W.WEIGHTS)
+        if a.warm_rules == "budget":
+            study_warmstart(range(lo, hi), a.weights or W.WEIGHTS, rules=BUDGET_RULES, uniform=False, noise=False)
+        else:
+            study_warmstart(range(lo, hi), a.weights or W.WEIGHTS)
         return 0
     if a.impl == "reference":
         return reference_arm(a, spec, run, desc, rank)

@@ -186,7 +186,8 @@ def _bf16_conv(torch):
             x, xr, w, wr = ctx.saved_tensors
             s, dyr = ctx.s, r(dy)
             dx = G.conv3d_input(x.shape, wr, dyr, stride=s, padding=1)
-            tc = dy.shape[-1] >= 16
+            bw = min(dy.shape[-1], 64)
+            tc = bw in (16, 32, 64) and dy.shape[-1] % bw == 0
             dw = G.conv3d_weight(xr if tc else x, w.shape, dyr if tc else dy, stride=s, padding=1)
             return dx, dw, dy.sum(dim=(0, 2, 3, 4)), None
 
