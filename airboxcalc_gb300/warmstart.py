@@ -11,8 +11,9 @@ moving, and falls back to the uniform start and the full schedule when they
 do not.  Training, inference and the initialisation run in the library's CUDA
 kernels; this module only moves parameters and drives the loop.
 
-Command line (trains on the GPU and writes the weights):
-    python -m airboxcalc_gb300.warmstart --train 0:2000 --epochs 20 --out weights.npz
+Command line (trains on the GPU and writes the weights; the defaults are the
+shipped network's recipe: 4000 seeded airboxes at dx 2 mm, 100 epochs):
+    python -m airboxcalc_gb300.warmstart --out weights.npz
 """
 from __future__ import annotations
 
@@ -220,14 +221,14 @@ def _range(s: str):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("--train", default="0:2000", help="seed range a:b of the training airboxes")
-    ap.add_argument("--val", default="5000:5032", help="seed range of the validation airboxes (loss only)")
+    ap.add_argument("--train", default="0:4000", help="seed range a:b of the training airboxes")
+    ap.add_argument("--val", default="5000:5064", help="seed range of the validation airboxes (loss only)")
     ap.add_argument("--dx", type=float, default=2.0)
     ap.add_argument("--res", type=int, default=64)
     ap.add_argument("--base", type=int, default=16)
     ap.add_argument("--levels", type=int, default=4)
     ap.add_argument("--coords", action="store_true", help="add the voxel coordinates as input channels")
-    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--epochs", type=int, default=100)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--lr-min", type=float, default=1e-5)
