@@ -478,13 +478,14 @@ def study_warmstart(seeds, weights: str, rules=WARM_RULES, uniform: bool = True,
     return summ, rows
 
 
-def batch_variants(n: int, seed0: int = 7000):
-    """The variant table of the batched run: seeded airboxes with dx in [2, 4) mm and K in {1.5, 3, 6}."""
+def batch_variants(n: int, seed0: int = 7000, dx_lo: float = 2.0, dx_hi: float = 4.0):
+    """The variant table of the batched run: seeded airboxes with dx in [dx_lo, dx_hi) mm (default [2, 4)) and K in
+    {1.5, 3, 6}."""
     from airboxcalc_gb300 import airboxgen as ag
     out = []
     for v in range(n):
         seed = seed0 + v
-        dx = round(2.0 + 2.0 * ((seed * 0.6180339887498949) % 1.0), 3)
+        dx = round(dx_lo + (dx_hi - dx_lo) * ((seed * 0.6180339887498949) % 1.0), 3)
         out.append((seed, ag.random_spec(seed, dx=dx), (1.5, 3.0, 6.0)[seed % 3], dx))
     return out
 
@@ -547,7 +548,7 @@ def study_net(batch: int = 8, iters: int = 10, modes=("f32", "tc"), res: int = 6
     return out
 
 
-def study_batch(n: int = 64, storage: str = "f16", quiet: bool = False):
+def study_batch(n: int = 64, storage: str = "f16", quiet: bool = False, dx_range=(2.0, 4.0)):
     """Batched variants: every seeded airbox alone in float32 (the reference's method, one solve at a
     time), alone in `storage`, and all together in one batched run (tuned shape, one launch per step).
     Reports aggregate MLUPS of each and each variant's KPI error against its float32 run."""
@@ -557,7 +558,7 @@ def study_batch(n: int = 64, storage: str = "f16", quiet: bool = False):
     geoms, params, rows, skipped = [], [], [], []
     t32 = t16 = 0.0
     cells = 0
-    for seed, spec, K, dx in batch_variants(n):
+    for seed, spec, K, dx in batch_variants(n, dx_lo=dx_range[0], dx_hi=dx_range[1]):
         run = dict(RUN, K=K)
         try:
             g = E.prepare({"tris": ag.build_airbox(spec), **spec.prepare_params(), "maxCells": 1e10})
@@ -595,7 +596,7 @@ def study_batch(n: int = 64, storage: str = "f16", quiet: bool = False):
         if not quiet:
             print(json.dumps(r), flush=True)
     upd = cells * RUN["steps"]
-    out = {"study": "batch", "variants": len(rows), "skipped_unstable_or_leaking": len(skipped),
+    out = {"study": "batch", "dx_mm": list(dx_range), "variants": len(rows), "skipped_unstable_or_leaking": len(skipped),
            "cells_min": min(r["NF"] for r in rows), "cells_max": max(r["NF"] for r in rows), "cells_total": cells,
            "storage": storage, "steps": RUN["steps"], "avg": RUN["avg"],
            "batched_mlups": round(upd / (info["run_ms"] * 1e-3) / 1e6, 1),
@@ -694,6 +695,7 @@ def main():
                          "KPIs, the learned warm start on held-out airboxes, the batched variant table, the "
                          "growth of the float32/float16 vs float64 field difference over a solve, or one "
                          "training step of the warm-start network on the float32 kernels and the tensor cores")
+    ap.add_argument("--batch-dx", default="2:4", help="--study batch: cell size range lo:hi (mm) of the variant table")
     ap.add_argument("--net-batch", type=int, default=8, help="batch of --study net")
     ap.add_argument("--net-iters", type=int, default=10, help="timed training steps of --study net")
     ap.add_argument("--net-modes", default="f32,tc", help="convolution paths of --study net")
@@ -716,7 +718,7 @@ def main():
         study_decorrelation(spec, run, desc)
         return 0
     if a.study == "batch":
-        study_batch(64, "f16")
+        study_batch(64, "f16", dx_range=tuple(float(v) for v in a.batch_dx.split(":")))
         return 0
     if a.study == "net":
         study_net(a.net_batch, a.net_iters, tuple(a.net_modes.split(",")))
