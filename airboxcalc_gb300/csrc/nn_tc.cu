@@ -59,8 +59,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
                : "memory");
   return ok != 0;
 }
-// Bounded wait (2^22 polls; a poll may suspend for a while, so this is seconds at most, far above any stage's copy
-// or MMA time).
+// Bounded wait: 2^22 polls, about 45 ms on GB300 (a launch whose first copies were never issued ended in 0.09 s
+// with its error flag set), three orders of magnitude above any stage's copy or MMA time.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   for (int i = 0; i < (1 << 22); i++)
     if (mbar_try_wait(bar, parity)) return true;
@@ -146,6 +146,7 @@ struct FwdArgs {
   int nchunk;            // K chunks per tap (Cin_pad * 2 / ROW)
   int relu, accum;
   int *err;              // set to 1 when a wait gave up
+  int drop;              // test hook: the K-step whose copies are never issued (-1: none), so that a wait runs out
 };
 
 // ROW: bytes of one operand row per chunk (32, 64 or 128: 16, 32 or 64 channels); N: Cout padded to 16.
@@ -187,6 +188,7 @@ __global__ void __launch_bounds__(128, 1) conv_fwd_kernel(const __grid_constant_
     for (int k = 0; k < nk; k++) {
       const int s = k % STAGES, use = k / STAGES;
       if (use > 0 && !mbar_wait(saddr(&empty[s]), (use - 1) & 1)) { fail = 1; break; }
+      if (k == p.drop) continue;
       const int tap = k / p.nchunk, ch = k % p.nchunk;
       const int kz = tap / 9, ky = (tap / 3) % 3, kx = tap % 3;
       const uint32_t a = saddr(smem + s * C::kStage), bb = a + C::kA, bar = saddr(&full[s]);
@@ -199,7 +201,8 @@ __global__ void __launch_bounds__(128, 1) conv_fwd_kernel(const __grid_constant_
     }
     // a stopped run waits (bounded) for the copies it started, so that none lands after the CTA has gone
     if (fail)
-      for (int k = armed > STAGES ? armed - STAGES : 0; k < armed; k++) mbar_wait(saddr(&full[k % STAGES]), (k / STAGES) & 1);
+      for (int k = armed > STAGES ? armed - STAGES : 0; k < armed; k++)
+        if (k != p.drop) mbar_wait(saddr(&full[k % STAGES]), (k / STAGES) & 1);
   } else if (warp == 1 && lane == 0) {
     // MMA issuer: ROW / 32 MMAs of K = 16 per chunk
     constexpr uint32_t id = idesc_bf16(128, N);
@@ -523,6 +526,9 @@ static int k_row(int cp) { return cp == 16 ? 32 : cp == 32 ? 64 : 128; }
 static int n_pad(int c) { return c <= 16 ? 16 : c <= 32 ? 32 : c <= 64 ? 64 : 128; }
 
 constexpr int kStages = 4;
+// Test hook of the forward kernel (FwdArgs::drop): -1 in every product path; the native check of the failure path
+// sets it to make one K-step's copies go missing.
+static int g_test_drop_kstep = -1;
 // pipeline depth of the weight-gradient kernel (its stages are small: one row of voxels each)
 #ifndef ABX_TC_WSTAGES
 #define ABX_TC_WSTAGES 4
@@ -603,7 +609,7 @@ static cudaError_t conv_forward(const float *x, int Cin, bool up2, const float *
   a.tw = (Wo + a.bw - 1) / a.bw; a.th = (Ho + a.bh - 1) / a.bh;
   const int td = (Do + a.bd - 1) / a.bd;
   a.nchunk = Kp * 2 / row;
-  a.relu = relu; a.accum = accum; a.err = sc.err;
+  a.relu = relu; a.accum = accum; a.err = sc.err; a.drop = g_test_drop_kstep;
   CUtensorMap mx, mw;
   {
     const cuuint64_t dims[5] = {(cuuint64_t)Kp, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)D, (cuuint64_t)B};

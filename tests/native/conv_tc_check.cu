@@ -9,10 +9,15 @@
 // input channels, the 4-channel linear head) and wide layers (64, 128 channels).  The weight gradient of layers
 // whose output rows are narrower than 16 voxels runs on the float32 kernels by design and is compared all the same.
 //
+// Then the failure path: with the forward kernel's test hook set, the copies of the first K-step are never issued,
+// so the MMA thread's bounded wait runs out; the launch must end by itself within seconds with the error flag set,
+// and the next (normal) launch must give the right result on the same context.
+//
 // Prints one line per layer and "all match" at the end; exit status 0 when every comparison passed.
 #include "nn.cu"
 #include "nn_tc.cu"
 
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -141,6 +146,41 @@ int main() {
     cudaFree(x); cudaFree(w); cudaFree(b); cudaFree(part);
     for (int k = 0; k < 2; k++) { cudaFree(y[k]); cudaFree(dy[k]); cudaFree(dx[k]); cudaFree(dw[k]); cudaFree(db[k]); }
     if (err) break;
+  }
+  // failure path (one small layer, four CTAs)
+  if (all) {
+    const Layer l{16, 16, 8, 1, 1};
+    const int D = l.D, Bf = 1;
+    const int64_t nx = (int64_t)Bf * l.Cin * D * D * D, ny = (int64_t)Bf * l.Cout * D * D * D, nw = (int64_t)l.Cout * l.Cin * 27;
+    const std::vector<float> hx = draw(nx, 1.0f), hw = draw(nw, 0.25f), hb = draw(l.Cout, 0.1f);
+    float *x, *w, *b, *y[2];
+    CK(cudaMalloc(&x, nx * 4)); CK(cudaMalloc(&w, nw * 4)); CK(cudaMalloc(&b, l.Cout * 4));
+    CK(cudaMalloc(&y[0], ny * 4)); CK(cudaMalloc(&y[1], ny * 4));
+    CK(cudaMemcpy(x, hx.data(), nx * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(w, hw.data(), nw * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b, hb.data(), l.Cout * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemset(sc.err, 0, sizeof(int)));
+    tc::g_test_drop_kstep = 0;
+    const auto t0 = std::chrono::steady_clock::now();
+    CK(nn_tc_conv3d(x, w, b, y[1], Bf, l.Cin, l.Cout, D, D, D, l.s, l.relu, 0, sc, 0));
+    CK(cudaDeviceSynchronize());
+    const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    tc::g_test_drop_kstep = -1;
+    int err = 0;
+    CK(cudaMemcpy(&err, sc.err, sizeof err, cudaMemcpyDeviceToHost));
+    printf("failure path: missing copies -> error flag %d after %.2f s\n", err, sec);
+    bool ok = err == 1;
+    CK(cudaMemset(sc.err, 0, sizeof(int)));
+    CK(nn_conv3d(x, w, b, y[0], Bf, l.Cin, l.Cout, D, D, D, l.s, l.relu, 0, 0));
+    CK(nn_tc_conv3d(x, w, b, y[1], Bf, l.Cin, l.Cout, D, D, D, l.s, l.relu, 0, sc, 0));
+    CK(cudaDeviceSynchronize());
+    CK(cudaMemcpy(&err, sc.err, sizeof err, cudaMemcpyDeviceToHost));
+    printf("failure path: next launch, error flag %d:", err);
+    ok &= err == 0;
+    ok &= compare("y", fetch(y[1], ny), fetch(y[0], ny));
+    printf("\n");
+    all &= ok;
+    cudaFree(x); cudaFree(w); cudaFree(b); cudaFree(y[0]); cudaFree(y[1]);
   }
   printf("worst rel_l2 %.2e\n%s\n", worst, all ? "all match" : "MISMATCH");
   return all ? 0 : 3;

@@ -3,7 +3,10 @@
 warm-start network through nn_tc.cu and through the float32 kernels of nn.cu
 with bfloat16-representable operands, where the two must agree to float32
 summation error (relative L2 < 1e-5) in the output, the data gradient, the
-weight gradient and the bias gradient."""
+weight gradient and the bias gradient; then the kernels' failure path: a
+forward launch whose first copies are never issued (a test hook) must end by
+itself with the error flag set, and the next launch on the same context must
+be right."""
 import os
 import shutil
 import subprocess
