@@ -325,6 +325,11 @@ def study_converge(spec, run, desc, storages=("f32", "f16", "bf16"), ladder=(600
 WARM_RULES = (dict(settle=1000, window=500, min_avg=1000, max_steps=4000, tol=0.01, rule=0, min_windows=4),
               dict(settle=500, window=250, min_avg=1000, max_steps=6000, tol=0.01, rule=1, min_windows=4),
               dict(settle=1000, window=500, min_avg=2000, max_steps=6000, tol=0.01, rule=1, min_windows=4))
+# Adaptive runs without the restart: the stop rule, and where it has not fired by max_steps the running average is
+# reported as it is (no fallback to the full schedule from f = w_i).
+ADAPTIVE_RULES = (dict(settle=500, window=250, min_avg=1000, max_steps=2500, tol=0.01, rule=1, min_windows=4, fallback=False),
+                  dict(settle=500, window=250, min_avg=1000, max_steps=3000, tol=0.01, rule=1, min_windows=4, fallback=False),
+                  dict(settle=750, window=250, min_avg=1000, max_steps=3000, tol=0.01, rule=0, min_windows=4, fallback=False))
 # Fixed step budgets (no stop test: a tolerance no window misses, two windows): settle S steps, then average A;
 # S + A = 1250, 1500, 2000 and 3000 steps, i.e. 4.8x, 4x, 3x and 2x fewer than the reference's 6000.
 BUDGET_RULES = tuple(dict(settle=s, window=a // 2, min_avg=a, max_steps=s + a, tol=1e9, rule=0, min_windows=2)
@@ -404,17 +409,43 @@ def study_warmstart(seeds, weights: str, rules=WARM_RULES, uniform: bool = True,
         del P
         S = E.Simulation(g, dict(run, storage="f16"))
         for i, rule in enumerate(rules):
-            W.solve_warm(S, net, **rule)
-            r = W.solve_warm(S, net, **rule)
-            eg, ez = _rel_err(r["metrics"], ref)
-            row[f"warm{i}"] = {"ms": round(r["total_ms"], 2), "steps": r["steps"], "fell_back": r["fell_back"],
-                               "infer_ms": round(r["infer_ms"], 3), "err_gammaCore": float(f"{eg:.3e}"),
-                               "err_zeta": float(f"{ez:.3e}")}
+            if rule.get("fallback", True):
+                rule = {k: v for k, v in rule.items() if k != "fallback"}
+                W.solve_warm(S, net, **rule)
+                r = W.solve_warm(S, net, **rule)
+                eg, ez = _rel_err(r["metrics"], ref)
+                row[f"warm{i}"] = {"ms": round(r["total_ms"], 2), "steps": r["steps"], "fell_back": r["fell_back"],
+                                   "infer_ms": round(r["infer_ms"], 3), "err_gammaCore": float(f"{eg:.3e}"),
+                                   "err_zeta": float(f"{ez:.3e}")}
+            else:
+                # warm start and convergence run, the running average reported even where the rule did not fire
+                rule = {k: v for k, v in rule.items() if k != "fallback"}
+                try:
+                    for timed in (False, True):
+                        S.reset()
+                        t0 = time.perf_counter()
+                        W.warm_start(S, net)
+                        r = W.converge(S, **rule)
+                        ms = (time.perf_counter() - t0) * 1e3
+                    fell = 0
+                except E.AirboxError:
+                    # the warm-started run went unstable: the reference's start and schedule, as solve_warm does
+                    # (the time counts the attempt that failed)
+                    t_fail = (time.perf_counter() - t0) * 1e3
+                    S.reset()
+                    t1 = time.perf_counter()
+                    S.run()
+                    r = {"metrics": S.evaluate()["metrics"], "steps": run["steps"], "converged": False}
+                    ms, fell = t_fail + (time.perf_counter() - t1) * 1e3, 1
+                eg, ez = _rel_err(r["metrics"], ref)
+                row[f"warm{i}"] = {"ms": round(ms, 2), "steps": r["steps"], "fell_back": fell, "converged": r["converged"],
+                                   "err_gammaCore": float(f"{eg:.3e}"), "err_zeta": float(f"{ez:.3e}")}
             if "ref_long" in row:
                 lg, lz = _rel_err(r["metrics"], row["ref_long"])
                 row[f"warm{i}"].update(err_long_gammaCore=float(f"{lg:.3e}"), err_long_zeta=float(f"{lz:.3e}"))
         if perfect:
             for i, rule in enumerate(rules):
+                rule = {k: v for k, v in rule.items() if k != "fallback"}
                 S.reset()
                 S.set_f(f_perfect)
                 W.converge(S, **rule)
@@ -427,7 +458,7 @@ def study_warmstart(seeds, weights: str, rules=WARM_RULES, uniform: bool = True,
                 row[f"perfect{i}"] = {"ms": round(ms, 2), "steps": r["steps"], "converged": r["converged"],
                                       "err_gammaCore": float(f"{eg:.3e}"), "err_zeta": float(f"{ez:.3e}")}
         if uniform:
-            rule = rules[0]
+            rule = {k: v for k, v in rules[0].items() if k != "fallback"}
             S.reset()
             W.converge(S, **rule)
             S.reset()
@@ -700,9 +731,10 @@ def main():
     ap.add_argument("--net-iters", type=int, default=10, help="timed training steps of --study net")
     ap.add_argument("--net-modes", default="f32,tc", help="convolution paths of --study net")
     ap.add_argument("--seeds", default="6000:6200", help="held-out seed range a:b of --study warmstart")
-    ap.add_argument("--warm-rules", default="stop", choices=["stop", "budget"],
-                    help="--study warmstart: the stop rules, or fixed step budgets (settle + average) without a stop "
-                         "test, which map the accuracy of the learned and of a perfect start against the budget")
+    ap.add_argument("--warm-rules", default="stop", choices=["stop", "budget", "adaptive"],
+                    help="--study warmstart: the stop rules with the restart fallback, fixed step budgets (settle + "
+                         "average) without a stop test, which map the accuracy of the learned and of a perfect start "
+                         "against the budget, or the stop rules without the restart")
     ap.add_argument("--storages", default="f64,f32exact,f32,f16,bf16", help="storages of --study precision")
     ap.add_argument("--weights", default=None, help="warm-start network weights (.npz)")
     a = ap.parse_args()
@@ -728,6 +760,9 @@ def main():
         lo, hi = map(int, a.seeds.split(":"))
         if a.warm_rules == "budget":
             study_warmstart(range(lo, hi), a.weights or W.WEIGHTS, rules=BUDGET_RULES, uniform=False, noise=False)
+        elif a.warm_rules == "adaptive":
+            study_warmstart(range(lo, hi), a.weights or W.WEIGHTS, rules=ADAPTIVE_RULES, uniform=False, noise=False,
+                            perfect=False)
         else:
             study_warmstart(range(lo, hi), a.weights or W.WEIGHTS)
         return 0
