@@ -311,8 +311,8 @@ void nn_tc_need(int B, int Cin, int Cout, int D, int s, TcNeed *n);
 int tc_wgrad_splits();
 cudaError_t nn_tc_conv3d(const float *x, const float *w, const float *b, float *y, int B, int Cin, int Cout, int D, int H,
                          int W, int s, int relu, int accum, const TcScratch &sc, cudaStream_t st);
-// as nn_conv3d_backward; part / part_floats: the float32 weight-gradient scratch for layers with rows under 16
-// voxels, which run on the float32 kernels
+// as nn_conv3d_backward; part / part_floats: the float32 weight-gradient scratch for the layers whose weight
+// gradient runs on the float32 kernels (output planes of fewer than 64 voxels)
 cudaError_t nn_tc_conv3d_backward(const float *x, const float *w, const float *y, float *dy, float *dx, float *dw,
                                   float *db, float *part, int64_t part_floats, int B, int Cin, int Cout, int D, int H,
                                   int W, int s, int relu, int accum_dx, const TcScratch &sc, cudaStream_t st);

@@ -74,6 +74,14 @@ __device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap *map
       "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
       : "memory");
 }
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      : "memory");
+}
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, uint32_t bar) {
   asm volatile(
       "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
@@ -257,11 +265,14 @@ __global__ void __launch_bounds__(128, 1) conv_fwd_kernel(const __grid_constant_
 struct WgradArgs {
   float *part;           // [nsplit][27][Cout][Cin]
   int Cout, Cin, Do, Ho, Wo, s;
-  int bw;                // voxels of one K-step (a row segment): Wo, at most 64
+  int bw;                // voxels of one K-step (a row segment): Wo, at most 64; 64 in the plane form
+  int plane;             // plane form (rows narrower than 16 voxels): a K-step is 64 consecutive voxels of an output
+                         // plane (64 / Wo whole rows), read through 4-D maps over flattened planes
+  int nyb;               // plane form: 64-voxel blocks per output plane
   int arows, brows;      // rows of the A and B boxes (Cout, min(Cin, N)); the tiles' other rows feed only
                          // accumulator rows and columns that are not stored
   int abytes, stage;     // bytes of a stage's A region (Cout rows, whole 1024-byte swizzle atoms) and of a stage
-  int rows;              // K-steps in all: B * Do * Ho * (Wo / bw)
+  int rows;              // K-steps in all: B * Do * Ho * (Wo / bw), or B * Do * nyb in the plane form
   int per;               // K-steps per CTA
   int *err;
 };
@@ -275,16 +286,21 @@ struct WgradCfg {
   static int smem(int abytes) { return STAGES * stage_bytes(abytes) + kSlack; }
 };
 
-// grid (27, nsplit); mapDY: channels-first dY {Wo, Ho, Do, Cout, B}, box {bw, 1, 1, Cout, 1}; mapXk: the input
-// copy for tap column k, shifted by k - 1 along W and decimated by s: {Wo, H, D, Cin, B}, box {bw, 1, 1, brows, 1}.
-// Each channel's box row is one K-major operand row of bw voxels (bw * 2 bytes = the swizzle span).  Rows of 8
-// voxels are not stacked into one K-step: a box of several 16-byte rows per channel does not land as one dense
-// operand row under the 128-byte swizzle (tried: wrong sums, and the largest such box wrote past the stage).
+// grid (27, nsplit).  Row form: mapDY is the channels-first dY {Wo, Ho, Do, Cout, B}, box {bw, 1, 1, Cout, 1};
+// mx.m[kx] the input copy for tap column kx, shifted by kx - 1 along W and decimated by s: {Wo, H, D, Cin, B}, box
+// {bw, 1, 1, brows, 1}.  Each channel's box row is one K-major operand row of bw voxels (bw * 2 bytes = the swizzle
+// span).  Plane form (rows of 8 voxels): dY as {Ho * Wo, Do, Cout, B}, box {64, 1, Cout, 1}, and mx.m[3 ky + kx] the
+// input copy shifted by (ky - 1, kx - 1) and decimated by s along H and W: {Ho * Wo, D, Cin, B}, box {64, 1, brows,
+// 1}: a K-step is 64 consecutive voxels of one output plane, again one 128-byte operand row per channel.  (Stacking
+// several 16-byte rows of a 5-D box into one K-step does not work: a box whose inner dimension is narrower than the
+// 128-byte swizzle span does not land as one dense operand row - tried: wrong sums, and the largest such box wrote
+// past the stage.)
+struct WgradMaps {
+  CUtensorMap m[9];
+};
 template <int ROW, int N, int STAGES>
 __global__ void __launch_bounds__(128, 1) conv_wgrad_kernel(const __grid_constant__ CUtensorMap mapDY,
-                                                            const __grid_constant__ CUtensorMap mapX0,
-                                                            const __grid_constant__ CUtensorMap mapX1,
-                                                            const __grid_constant__ CUtensorMap mapX2, const WgradArgs p) {
+                                                            const __grid_constant__ WgradMaps mx, const WgradArgs p) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long full[STAGES], empty[STAGES], accf;
   __shared__ uint32_t tmem_base;
@@ -293,7 +309,7 @@ __global__ void __launch_bounds__(128, 1) conv_wgrad_kernel(const __grid_constan
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tap = blockIdx.x, split = blockIdx.y;
   const int kz = tap / 9, ky = (tap / 3) % 3, kx = tap % 3;
-  const CUtensorMap *mapX = kx == 0 ? &mapX0 : kx == 1 ? &mapX1 : &mapX2;
+  const CUtensorMap *mapX = &mx.m[p.plane ? 3 * ky + kx : kx];
   const int k0 = split * p.per, k1 = p.rows < k0 + p.per ? p.rows : k0 + p.per;
   const int nk = k1 > k0 ? k1 - k0 : 0;
   const int nwb = p.Wo / p.bw;
@@ -313,12 +329,18 @@ __global__ void __launch_bounds__(128, 1) conv_wgrad_kernel(const __grid_constan
     for (int k = 0; k < nk; k++) {
       const int s = k % STAGES, use = k / STAGES;
       if (use > 0 && !mbar_wait(saddr(&empty[s]), (use - 1) & 1)) { fail = 1; break; }
-      const int r = k0 + k;                     // (b, oz, oy, x-chunk) of the K-step
-      const int xc = r % nwb, oy = (r / nwb) % p.Ho, oz = (r / (nwb * p.Ho)) % p.Do, b = r / (nwb * p.Ho * p.Do);
+      const int r = k0 + k;
       const uint32_t a = saddr(smem + s * p.stage), bb = a + p.abytes, bar = saddr(&full[s]);
       mbar_expect_tx(bar, (uint32_t)((p.arows + p.brows) * ROW));
-      tma_load_5d(a, &mapDY, xc * p.bw, oy, oz, 0, b, bar);
-      tma_load_5d(bb, mapX, xc * p.bw, oy * p.s + ky - 1, oz * p.s + kz - 1, 0, b, bar);
+      if (p.plane) {                            // (b, oz, 64-voxel block of the plane)
+        const int yb = r % p.nyb, oz = (r / p.nyb) % p.Do, b = r / (p.nyb * p.Do);
+        tma_load_4d(a, &mapDY, yb * 64, oz, 0, b, bar);
+        tma_load_4d(bb, mapX, yb * 64, oz * p.s + kz - 1, 0, b, bar);
+      } else {                                  // (b, oz, oy, x-chunk)
+        const int xc = r % nwb, oy = (r / nwb) % p.Ho, oz = (r / (nwb * p.Ho)) % p.Do, b = r / (nwb * p.Ho * p.Do);
+        tma_load_5d(a, &mapDY, xc * p.bw, oy, oz, 0, b, bar);
+        tma_load_5d(bb, mapX, xc * p.bw, oy * p.s + ky - 1, oz * p.s + kz - 1, 0, b, bar);
+      }
       armed = k + 1;
     }
     if (fail)
@@ -413,6 +435,30 @@ __global__ void to_cf_shift_kernel(const float *__restrict__ x, __nv_bfloat16 *_
     for (int kx = 0; kx < 3; kx++) {
       const int src = s * (int)w + kx - 1;
       ob[kx * n + j] = __float2bfloat16_rn((src >= 0 && src < W) ? xr[src] : 0.0f);
+    }
+  }
+}
+
+// x [B][C][D][H][W] float32 -> nine bf16 copies [9][B][C][D][Ho][Wo]: copy 3 ky + kx holds
+// x[..][s * oy + ky - 1][s * ox + kx - 1] (zero outside the grid).  n = B * C * D * Ho * Wo (the copies' stride); grid
+// (blocks, B), indices within a sample 32-bit (the host checks C * D * H * W < 2^31).
+__global__ void to_cf_shift9_kernel(const float *__restrict__ x, __nv_bfloat16 *__restrict__ out, int64_t n,
+                                    uint32_t planes, int H, int W, int Ho, int Wo, int s) {
+  const uint32_t pl = (uint32_t)Ho * Wo, m = planes * pl;   // one sample's elements per copy
+  const float *xb = x + (int64_t)blockIdx.y * planes * H * W;
+  __nv_bfloat16 *ob = out + (int64_t)blockIdx.y * m;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
+    const uint32_t q = j / pl, r = j % pl, oy = r / (uint32_t)Wo, ox = r % (uint32_t)Wo;
+    const float *xp = xb + (size_t)q * H * W;
+#pragma unroll
+    for (int ky = 0; ky < 3; ky++) {
+      const int yy = s * (int)oy + ky - 1;
+#pragma unroll
+      for (int kx = 0; kx < 3; kx++) {
+        const int xx = s * (int)ox + kx - 1;
+        const bool in = yy >= 0 && yy < H && xx >= 0 && xx < W;
+        ob[(3 * ky + kx) * n + j] = __float2bfloat16_rn(in ? xp[(size_t)yy * W + xx] : 0.0f);
+      }
     }
   }
 }
@@ -560,7 +606,7 @@ static cudaError_t launch_fwd_n(int N, const CUtensorMap &mx, const CUtensorMap 
 }
 
 template <int ROW, int N>
-static cudaError_t launch_wgrad(const CUtensorMap &mdy, const CUtensorMap *mx, const WgradArgs &a, dim3 grid,
+static cudaError_t launch_wgrad(const CUtensorMap &mdy, const WgradMaps &mx, const WgradArgs &a, dim3 grid,
                                 cudaStream_t st) {
   using C = WgradCfg<ROW, N, kWStages>;
   const int smem = C::smem(a.abytes);
@@ -573,11 +619,11 @@ static cudaError_t launch_wgrad(const CUtensorMap &mdy, const CUtensorMap *mx, c
   }
   WgradArgs b = a;
   b.stage = C::stage_bytes(a.abytes);
-  conv_wgrad_kernel<ROW, N, kWStages><<<grid, 128, smem, st>>>(mdy, mx[0], mx[1], mx[2], b);
+  conv_wgrad_kernel<ROW, N, kWStages><<<grid, 128, smem, st>>>(mdy, mx, b);
   return cudaGetLastError();
 }
 template <int ROW>
-static cudaError_t launch_wgrad_n(int N, const CUtensorMap &mdy, const CUtensorMap *mx, const WgradArgs &a, dim3 grid,
+static cudaError_t launch_wgrad_n(int N, const CUtensorMap &mdy, const WgradMaps &mx, const WgradArgs &a, dim3 grid,
                                   cudaStream_t st) {
   switch (N) {
     case 16: return launch_wgrad<ROW, 16>(mdy, mx, a, grid, st);
@@ -659,7 +705,7 @@ void nn_tc_need(int B, int Cin, int Cout, int D, int s, TcNeed *n) {
   const int kf = tc::k_pad(Cin), kb = tc::k_pad(Cout);
   n->cl_elems = std::max(n->cl_elems, (int64_t)B * V * std::max(kf, kb));
   n->w_elems = std::max(n->w_elems, (int64_t)27 * std::max(tc::n_pad(Cout) * kf, tc::n_pad(Cin) * kb));
-  n->xs_elems = std::max(n->xs_elems, (int64_t)3 * B * Cin * D * D * Do);
+  n->xs_elems = std::max(n->xs_elems, std::max((int64_t)3 * B * Cin * D * D * Do, (int64_t)9 * B * Cin * D * Do * Do));
   n->dyc_elems = std::max(n->dyc_elems, (int64_t)B * Cout * Vo);
   n->part_floats = std::max(n->part_floats, (int64_t)std::max(tc_wgrad_splits() * 27 * Cin, tc::kBiasParts) * Cout);
 }
@@ -685,39 +731,62 @@ cudaError_t nn_tc_conv3d_backward(const float *x, const float *w, const float *y
     cudaError_t e = tc::conv_forward(dy, Cout, s == 2, w, true, nullptr, dx, B, Cin, D, H, W, 1, 0, accum_dx, sc, st);
     if (e != cudaSuccess) return e;
   }
-  // weight and bias gradients: K-steps of one row segment of 16, 32 or 64 voxels
+  // weight and bias gradients: K-steps of one row segment of 16, 32 or 64 voxels (row form), or of 64 voxels of an
+  // output plane of rows narrower than 16 voxels (plane form)
   const int bw = std::min(Wo, 64);
-  if (Cout <= 128 && (bw == 16 || bw == 32 || bw == 64) && Wo % bw == 0) {
-    const int N = tc::n_pad(Cin), row = bw * 2;
-    if ((int64_t)3 * B * Cin * D * H * Wo > sc.xs_elems || (int64_t)B * Cout * Vo > sc.dyc_elems) return cudaErrorInvalidValue;
-    tc::to_bf16_kernel<<<tc::blocks_for((int64_t)B * Cout * Vo), 256, 0, st>>>(dy, sc.dyc, (int64_t)B * Cout * Vo);
-    const int64_t rows_x = (int64_t)B * Cin * D * H;
+  const bool row_form = (bw == 16 || bw == 32 || bw == 64) && Wo % bw == 0;
+  const bool plane_form = !row_form && Wo < 16 && (Ho * Wo) % 64 == 0;
+  if (Cout <= 128 && (row_form || plane_form)) {
+    const int N = tc::n_pad(Cin), row = row_form ? bw * 2 : 128;
+    const int64_t nxs = row_form ? (int64_t)3 * B * Cin * D * H * Wo : (int64_t)9 * B * Cin * D * Ho * Wo;
+    if (nxs > sc.xs_elems || (int64_t)B * Cout * Vo > sc.dyc_elems) return cudaErrorInvalidValue;
     if ((int64_t)Cin * D * H * W >= (1ll << 31)) return cudaErrorInvalidValue;
-    tc::to_cf_shift_kernel<<<dim3(tc::blocks_for(rows_x / B * Wo), (unsigned)B), 256, 0, st>>>(
-        x, sc.xs, rows_x * Wo, (uint32_t)(rows_x / B), W, Wo, s);
-    CUtensorMap mdy, mx[3];
-    {
+    tc::to_bf16_kernel<<<tc::blocks_for((int64_t)B * Cout * Vo), 256, 0, st>>>(dy, sc.dyc, (int64_t)B * Cout * Vo);
+    CUtensorMap mdy{};
+    tc::WgradMaps mx{};
+    const cuuint32_t brows = (cuuint32_t)std::min(Cin, N);
+    if (row_form) {
+      const int64_t rows_x = (int64_t)B * Cin * D * H;
+      tc::to_cf_shift_kernel<<<dim3(tc::blocks_for(rows_x / B * Wo), (unsigned)B), 256, 0, st>>>(
+          x, sc.xs, rows_x * Wo, (uint32_t)(rows_x / B), W, Wo, s);
       const cuuint64_t dims[5] = {(cuuint64_t)Wo, (cuuint64_t)Ho, (cuuint64_t)Do, (cuuint64_t)Cout, (cuuint64_t)B};
       const cuuint64_t strides[4] = {(cuuint64_t)Wo * 2, (cuuint64_t)Wo * Ho * 2, (cuuint64_t)Vo * 2, (cuuint64_t)Vo * Cout * 2};
       const cuuint32_t box[5] = {(cuuint32_t)bw, 1, 1, (cuuint32_t)Cout, 1};
       const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
       cudaError_t e = tc::make_map(&mdy, sc.dyc, 5, dims, strides, box, estr, row);
       if (e != cudaSuccess) return e;
-    }
-    for (int kx = 0; kx < 3; kx++) {
-      const cuuint64_t dims[5] = {(cuuint64_t)Wo, (cuuint64_t)H, (cuuint64_t)D, (cuuint64_t)Cin, (cuuint64_t)B};
-      const cuuint64_t strides[4] = {(cuuint64_t)Wo * 2, (cuuint64_t)Wo * H * 2, (cuuint64_t)Wo * H * D * 2,
-                                     (cuuint64_t)Wo * H * D * Cin * 2};
-      const cuuint32_t box[5] = {(cuuint32_t)bw, 1, 1, (cuuint32_t)std::min(Cin, N), 1};
-      const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
-      cudaError_t e = tc::make_map(&mx[kx], sc.xs + (int64_t)kx * rows_x * Wo, 5, dims, strides, box, estr, row);
+      for (int kx = 0; kx < 3; kx++) {
+        const cuuint64_t xdims[5] = {(cuuint64_t)Wo, (cuuint64_t)H, (cuuint64_t)D, (cuuint64_t)Cin, (cuuint64_t)B};
+        const cuuint64_t xstrides[4] = {(cuuint64_t)Wo * 2, (cuuint64_t)Wo * H * 2, (cuuint64_t)Wo * H * D * 2,
+                                        (cuuint64_t)Wo * H * D * Cin * 2};
+        const cuuint32_t xbox[5] = {(cuuint32_t)bw, 1, 1, brows, 1};
+        e = tc::make_map(&mx.m[kx], sc.xs + (int64_t)kx * rows_x * Wo, 5, xdims, xstrides, xbox, estr, row);
+        if (e != cudaSuccess) return e;
+      }
+    } else {
+      const int64_t n9 = (int64_t)B * Cin * D * Ho * Wo, pl = (int64_t)Ho * Wo;
+      tc::to_cf_shift9_kernel<<<dim3(tc::blocks_for(n9 / B), (unsigned)B), 256, 0, st>>>(
+          x, sc.xs, n9, (uint32_t)(Cin * D), H, W, Ho, Wo, s);
+      const cuuint64_t dims[4] = {(cuuint64_t)pl, (cuuint64_t)Do, (cuuint64_t)Cout, (cuuint64_t)B};
+      const cuuint64_t strides[3] = {(cuuint64_t)pl * 2, (cuuint64_t)Vo * 2, (cuuint64_t)Vo * Cout * 2};
+      const cuuint32_t box[4] = {64, 1, (cuuint32_t)Cout, 1};
+      const cuuint32_t estr[4] = {1, 1, 1, 1};
+      cudaError_t e = tc::make_map(&mdy, sc.dyc, 4, dims, strides, box, estr, row);
       if (e != cudaSuccess) return e;
+      for (int c = 0; c < 9; c++) {
+        const cuuint64_t xdims[4] = {(cuuint64_t)pl, (cuuint64_t)D, (cuuint64_t)Cin, (cuuint64_t)B};
+        const cuuint64_t xstrides[3] = {(cuuint64_t)pl * 2, (cuuint64_t)pl * D * 2, (cuuint64_t)pl * D * Cin * 2};
+        const cuuint32_t xbox[4] = {64, 1, brows, 1};
+        e = tc::make_map(&mx.m[c], sc.xs + (int64_t)c * n9, 4, xdims, xstrides, xbox, estr, row);
+        if (e != cudaSuccess) return e;
+      }
     }
     tc::WgradArgs a{};
-    a.part = sc.part; a.Cout = Cout; a.Cin = Cin; a.Do = Do; a.Ho = Ho; a.Wo = Wo; a.s = s; a.bw = bw;
+    a.part = sc.part; a.Cout = Cout; a.Cin = Cin; a.Do = Do; a.Ho = Ho; a.Wo = Wo; a.s = s; a.bw = row_form ? bw : 64;
+    a.plane = plane_form ? 1 : 0; a.nyb = plane_form ? Ho * Wo / 64 : 0;
     a.arows = Cout; a.brows = std::min(Cin, N);
     a.abytes = (Cout * row + 1023) / 1024 * 1024;
-    a.rows = B * Do * Ho * (Wo / bw);
+    a.rows = plane_form ? B * Do * a.nyb : B * Do * Ho * (Wo / bw);
     const int nsplit = std::min(tc_wgrad_splits(), a.rows);
     a.per = (a.rows + nsplit - 1) / nsplit;
     a.err = sc.err;
@@ -737,7 +806,8 @@ cudaError_t nn_tc_conv3d_backward(const float *x, const float *w, const float *y
     tc::bias_sum_kernel<<<(Cout + 127) / 128, 128, 0, st>>>(sc.part, db, Cout);
     return cudaGetLastError();
   }
-  // rows narrower than 16 voxels: the float32 kernels (the ReLU mask is already applied)
+  // other shapes (planes of fewer than 64 voxels, more than 128 output channels): the float32 kernels (the ReLU
+  // mask is already applied)
   return nn_conv3d_backward(x, w, y, dy, nullptr, dw, db, part, part_floats, B, Cin, Cout, D, H, W, s, 0, 0, st);
 }
 

@@ -165,8 +165,10 @@ def _bf16_conv(torch):
     the way the tensor-core path does: the forward rounds x and w; the data
     gradient rounds the (ReLU-masked) output gradient and w; the weight
     gradient rounds the output gradient and x where that path computes it on
-    the tensor cores (output rows of at least 16 voxels) and keeps float32
-    operands elsewhere; the bias gradient sums the unrounded output gradient."""
+    the tensor cores (output rows of 16, 32 or a multiple of 64 voxels, or
+    narrower rows in output planes of a multiple of 64 voxels) and keeps
+    float32 operands elsewhere; the bias gradient sums the unrounded output
+    gradient."""
     F = torch.nn.functional
     G = torch.nn.grad
 
@@ -186,8 +188,9 @@ def _bf16_conv(torch):
             x, xr, w, wr = ctx.saved_tensors
             s, dyr = ctx.s, r(dy)
             dx = G.conv3d_input(x.shape, wr, dyr, stride=s, padding=1)
-            bw = min(dy.shape[-1], 64)
-            tc = bw in (16, 32, 64) and dy.shape[-1] % bw == 0
+            wo, ho = dy.shape[-1], dy.shape[-2]
+            bw = min(wo, 64)
+            tc = (bw in (16, 32, 64) and wo % bw == 0) or (wo < 16 and (ho * wo) % 64 == 0)
             dw = G.conv3d_weight(xr if tc else x, w.shape, dyr if tc else dy, stride=s, padding=1)
             return dx, dw, dy.sum(dim=(0, 2, 3, 4)), None
 

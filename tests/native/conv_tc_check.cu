@@ -7,7 +7,7 @@
 //
 // Shapes: every convolution of the warm-start network at 8^3 .. 64^3 (bases 8 and 16, strides 1 and 2, 9 and 12
 // input channels, the 4-channel linear head) and wide layers (64, 128 channels).  The weight gradient of layers
-// whose output rows are narrower than 16 voxels runs on the float32 kernels by design and is compared all the same.
+// whose output planes hold fewer than 64 voxels runs on the float32 kernels by design and is compared all the same.
 //
 // Then the failure path: with the forward kernel's test hook set, the copies of the first K-step are never issued,
 // so the MMA thread's bounded wait runs out; the launch must end by itself within seconds with the error flag set,
