@@ -872,13 +872,13 @@ def ours_arm(a, spec, run, desc, ws, rank, local):
     if rank == 0 and not a.no_warm_start:
         from airboxcalc_gb300 import warmstart as W
         if os.path.exists(W.WEIGHTS):
-            summ, _ = study_warmstart(range(6000, 6012), W.WEIGHTS, rules=WARM_RULES[:1], uniform=False,
+            summ, _ = study_warmstart(range(6000, 6048), W.WEIGHTS, rules=WARM_RULES[:1], uniform=False,
                                       noise=False, perfect=False, quiet=True)
             w = summ["warm0_f16"]
             line["warm_start"] = {
                 "what": "time to converged gamma core / zeta: float16 + learned warm start + convergence run vs the "
                         "plain float32 run (6000/2000 steps), host wall time per solve, held-out seeded airboxes "
-                        "6000-6011 at dx 2 mm (the full 200-seed study: bench.py --study warmstart)",
+                        "6000-6047 at dx 2 mm (the full 200-seed study: bench.py --study warmstart)",
                 "airboxes": w["n"], "median_speedup_vs_plain_f32": w["median_speedup_vs_plain_f32"],
                 "within_1pct_both_kpis": w["within_1pct"], "median_err_gammaCore": w["median_err_gammaCore"],
                 "median_err_zeta": w["median_err_zeta"], "fallback_rate": w["fallback_rate"],
