@@ -73,8 +73,9 @@ __device__ __forceinline__ void step_cells(const Args &a, const uint2 (&sg)[SPW]
     // 32-bit element indices: the host guarantees 19 * Np < 2^32
     p[j] = seg_base(sg[j]) + lane;
     // in flight together with the population loads below; known without a load in the interior segments of
-    // an odd step (even steps keep the plain load: their 16-bit kernels have no register to spare for the branch)
-    m[j] = act[j] ? ((ODD && (sg[j].x & kSegInterior)) ? kMaskInterior : a.mask[p[j]]) : 0u;
+    // an odd step, and of an even step for the float32 storage (the 16-bit even steps keep the plain load: they
+    // have no register to spare for the branch)
+    m[j] = act[j] ? (((ODD || K == kStoreF32) && (sg[j].x & kSegInterior)) ? kMaskInterior : a.mask[p[j]]) : 0u;
     if (!act[j]) continue;
     if (ODD) {
       // Pull from the neighbours first.  For a fluid cell x every x - c_q lies
