@@ -530,6 +530,28 @@ __global__ void relu_mask_kernel(const float *__restrict__ y, float *__restrict_
     if (!(y[i] > 0.0f)) dy[i] = 0.0f;
 }
 
+// The output gradient's ReLU mask (when y is given) and its bf16 copy for the weight gradient in one pass, four
+// elements per thread (n a multiple of 4, 16-byte aligned buffers: the host checks): dy[i] = 0 where y[i] <= 0,
+// out[i] = bf16(dy[i]).
+__global__ void mask_bf16_kernel(const float *__restrict__ y, float *__restrict__ dy, __nv_bfloat16 *__restrict__ out,
+                                 int64_t n4) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+    float4 d = reinterpret_cast<const float4 *>(dy)[i];
+    if (y) {
+      const float4 v = reinterpret_cast<const float4 *>(y)[i];
+      const bool keep = (v.x > 0.0f) && (v.y > 0.0f) && (v.z > 0.0f) && (v.w > 0.0f);
+      if (!keep) {
+        d.x = v.x > 0.0f ? d.x : 0.0f; d.y = v.y > 0.0f ? d.y : 0.0f;
+        d.z = v.z > 0.0f ? d.z : 0.0f; d.w = v.w > 0.0f ? d.w : 0.0f;
+        reinterpret_cast<float4 *>(dy)[i] = d;
+      }
+    }
+    __align__(8) __nv_bfloat16 q[4] = {__float2bfloat16_rn(d.x), __float2bfloat16_rn(d.y), __float2bfloat16_rn(d.z),
+                                       __float2bfloat16_rn(d.w)};
+    reinterpret_cast<uint2 *>(out)[i] = *reinterpret_cast<const uint2 *>(q);
+  }
+}
+
 // ======================================================================== host side
 static unsigned blocks_for(int64_t n) {
   int64_t b = (n + 255) / 256;
@@ -727,7 +749,19 @@ cudaError_t nn_tc_conv3d_backward(const float *x, const float *w, const float *y
   if (s == 2 && ((D | H | W) & 1)) return cudaErrorInvalidValue;
   const int Do = (D - 1) / s + 1, Ho = (H - 1) / s + 1, Wo = (W - 1) / s + 1;
   const int64_t Vo = (int64_t)Do * Ho * Wo;
-  if (relu) tc::relu_mask_kernel<<<tc::blocks_for((int64_t)B * Cout * Vo), 256, 0, st>>>(y, dy, (int64_t)B * Cout * Vo);
+  const int bw = std::min(Wo, 64);
+  const bool row_form = (bw == 16 || bw == 32 || bw == 64) && Wo % bw == 0;
+  const bool plane_form = !row_form && Wo < 16 && (Ho * Wo) % 64 == 0;
+  const bool tc_wgrad = Cout <= 128 && (row_form || plane_form);
+  const int64_t ny = (int64_t)B * Cout * Vo;
+  // ReLU mask and (for the tensor-core weight gradient) the bf16 copy of the output gradient: one vectorised pass
+  // where the sizes and addresses allow, else two
+  const bool fused = tc_wgrad && ny % 4 == 0 && ny <= sc.dyc_elems &&
+                     (((uintptr_t)dy | (uintptr_t)y | (uintptr_t)sc.dyc) & 15) == 0;
+  if (fused)
+    tc::mask_bf16_kernel<<<tc::blocks_for(ny / 4), 256, 0, st>>>(relu ? y : nullptr, dy, sc.dyc, ny / 4);
+  else if (relu)
+    tc::relu_mask_kernel<<<tc::blocks_for(ny), 256, 0, st>>>(y, dy, ny);
   // data gradient: the forward kernel on dy (zero-inserted for stride 2) with flipped, transposed weights
   if (dx) {
     cudaError_t e = tc::conv_forward(dy, Cout, s == 2, w, true, nullptr, dx, B, Cin, D, H, W, 1, 0, accum_dx, sc, st);
@@ -735,15 +769,12 @@ cudaError_t nn_tc_conv3d_backward(const float *x, const float *w, const float *y
   }
   // weight and bias gradients: K-steps of one row segment of 16, 32 or 64 voxels (row form), or of 64 voxels of an
   // output plane of rows narrower than 16 voxels (plane form)
-  const int bw = std::min(Wo, 64);
-  const bool row_form = (bw == 16 || bw == 32 || bw == 64) && Wo % bw == 0;
-  const bool plane_form = !row_form && Wo < 16 && (Ho * Wo) % 64 == 0;
-  if (Cout <= 128 && (row_form || plane_form)) {
+  if (tc_wgrad) {
     const int N = tc::n_pad(Cin), row = row_form ? bw * 2 : 128;
     const int64_t nxs = row_form ? (int64_t)3 * B * Cin * D * H * Wo : (int64_t)9 * B * Cin * D * Ho * Wo;
     if (nxs > sc.xs_elems || (int64_t)B * Cout * Vo > sc.dyc_elems) return cudaErrorInvalidValue;
     if ((int64_t)Cin * D * H * W >= (1ll << 31)) return cudaErrorInvalidValue;
-    tc::to_bf16_kernel<<<tc::blocks_for((int64_t)B * Cout * Vo), 256, 0, st>>>(dy, sc.dyc, (int64_t)B * Cout * Vo);
+    if (!fused) tc::to_bf16_kernel<<<tc::blocks_for(ny), 256, 0, st>>>(dy, sc.dyc, ny);
     CUtensorMap mdy{};
     tc::WgradMaps mx{};
     const cuuint32_t brows = (cuuint32_t)std::min(Cin, N);
