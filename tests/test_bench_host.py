@@ -45,3 +45,33 @@ def test_reference_arm_prints_one_line():
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["unit"] == "MLUPS" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_network_flop_count_matches_the_layer_list():
+    """bench.net_flops (the multiply-adds behind --study net's TFLOP/s) against the network's layer list in the
+    restatement: forward, data gradient (not for the first layer) and weight gradient of every convolution."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from oracle import warmstart_ref as R_
+    for res, base, levels, batch in ((64, 16, 4, 8), (32, 8, 2, 2), (16, 8, 3, 1)):
+        out_res = []
+        for l in range(levels):
+            out_res += [res >> l] * 2
+        for l in range(levels - 2, -1, -1):
+            out_res += [res >> l] * 2
+        out_res.append(res)
+        layers = R_.conv_layers(base, levels)
+        assert len(layers) == len(out_res)
+        want = sum(2.0 * 27 * cin * cout * d ** 3 * batch * (2 if i == 0 else 3)
+                   for i, ((cin, cout, s, relu), d) in enumerate(zip(layers, out_res)))
+        assert bench.net_flops(res, base, levels, batch) == pytest.approx(want, rel=1e-12)
+
+
+def test_fixed_budget_rules_run_exactly_their_budget():
+    """--warm-rules budget: two windows of A/2 steps after S settling steps, a tolerance no window misses."""
+    sys.path.insert(0, ROOT)
+    import bench
+    for r in bench.BUDGET_RULES:
+        assert r["max_steps"] == r["settle"] + 2 * r["window"] == r["settle"] + r["min_avg"]
+        assert r["rule"] == 0 and r["tol"] > 1e6
+    assert [r["settle"] + r["min_avg"] for r in bench.BUDGET_RULES] == [1250, 1500, 2000, 3000]
