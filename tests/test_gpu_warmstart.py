@@ -238,13 +238,17 @@ CZ = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1])
 
 def test_trained_network_beats_the_uniform_start():
     """What the shipped, trained network gains over the same method without it, on held-out airboxes
-    (seeds 6000-6011 of the generator at dx 2 mm; training used seeds 0-1999):
+    (seeds 6000-6011 of the generator at dx 2 mm; training used seeds 0-3999):
 
     * its start is much closer to the plain float32 run's time-averaged velocity than the uniform start
       f = w_i, whose velocity is zero (relative L2 error exactly 1);
     * the same float16 convergence run (default stop rule) ends with smaller gamma core / zeta errors
       against the plain float32 run on the reference's 6000/2000 schedule when it starts from the network's
       prediction (abx_sim_solve_warm) than when it starts from f = w_i (abx_sim_converge after a reset).
+
+    Measured with the shipped network (11 stable airboxes): start error 0.19-0.29 (median 0.25); KPI error after
+    the run median 1.5 % warm against 12 % uniform; 4 warm runs and no uniform run within 1 %.  The bounds leave
+    room for rounding differences between GPUs, not for a network that stopped helping.
     """
     net = W.Net.load()
     start_err, warm_err, uniform_err = [], [], []
@@ -273,7 +277,10 @@ def test_trained_network_beats_the_uniform_start():
         S.reset()
         uniform_err.append(err(W.converge(S)["metrics"]))
         del S, g
+    print("start error", np.round(start_err, 3), "\nwarm KPI error", np.round(warm_err, 4),
+          "\nuniform KPI error", np.round(uniform_err, 4))
     assert len(warm_err) >= 6, "too few stable held-out airboxes"
-    assert np.median(start_err) < 0.6, start_err
-    assert np.median(warm_err) < np.median(uniform_err), (warm_err, uniform_err)
-    assert sum(e < 0.01 for e in warm_err) >= sum(e < 0.01 for e in uniform_err), (warm_err, uniform_err)
+    assert np.median(start_err) < 0.35, start_err
+    assert np.median(warm_err) < 0.25 * np.median(uniform_err), (warm_err, uniform_err)
+    n_warm, n_uniform = sum(e < 0.01 for e in warm_err), sum(e < 0.01 for e in uniform_err)
+    assert n_warm >= 3 and n_warm > n_uniform, (warm_err, uniform_err)
